@@ -1,0 +1,219 @@
+"""Pins the CPU oracle against known-answer physics (the reference ships no
+golden vectors: test/runtests.jl is an empty testset)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import exact as X
+
+
+def tfim(N, J=1.0, h=0.5):
+    H = O.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], -J)
+    for i in range(1, N + 1):
+        H.add("x", i, -h)
+    return H
+
+
+def xxz(N, J=1.0, delta=1.0, field=None):
+    H = O.OpList(N)
+    for i in range(1, N):
+        H.add(["x", "x"], [i, i + 1], J)
+        H.add(["y", "y"], [i, i + 1], J)
+        H.add(["z", "z"], [i, i + 1], J * delta)
+    if field is not None:
+        for i in range(1, N + 1):
+            H.add("z", i, field(i))
+    return H
+
+
+def test_free_fermion_formula_matches_ed():
+    st = O.spinhalf()
+    N = 8
+    E_ed = np.linalg.eigvalsh(X.oplist_to_dense(st, tfim(N)))[0]
+    assert abs(X.tfim_free_fermion_energy(N, 1.0, 0.5) - E_ed) < 1e-11
+
+
+@pytest.mark.parametrize("which", ["tfim", "xxz", "xxz_field"])
+def test_mpo_builder_matches_dense(which):
+    st = O.spinhalf()
+    N = 6
+    H = {"tfim": tfim(N), "xxz": xxz(N), "xxz_field": xxz(N, 1.0, 0.5, lambda i: 0.2 * (-1) ** i)}[which]
+    W = O.mpo_from_oplist(st, H)
+    dense = X.oplist_to_dense(st, H)
+    assert np.allclose(X.mpo_to_dense(W), dense, atol=1e-12)
+    w = max(W[i].shape[3] for i in range(1, N))
+    assert w == {"tfim": 3, "xxz": 5, "xxz_field": 5}[which]
+
+
+def test_svd_keep_rule():
+    S = np.array([1.0, 0.5, 1e-3, 1e-6, 0.0])
+    assert O.svd_keep(S) == 5                     # no cutoff: zeros kept
+    assert O.svd_keep(S, maxdim=2) == 2
+    assert O.svd_keep(S, cutoff=1e-8) == 3         # tail from 4 holds 1e-12/1.25
+    assert O.svd_keep(S, cutoff=1e-13) == 4
+    assert O.svd_keep(S, cutoff=0.9) == 1
+    assert O.svd_keep(S, cutoff=0.9, mindim=3) == 3
+    assert O.svd_keep(np.zeros(3), cutoff=1e-10) == 1
+
+
+def test_lanczos_converges_to_lowest():
+    rng = np.random.default_rng(0)
+    n = 40
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = A + A.conj().T
+    x0 = rng.standard_normal(n) + 0j
+    e, v = O.lanczos_lowest(lambda x: A @ x, x0, 20, 30)
+    assert abs(e - np.linalg.eigvalsh(A)[0]) < 1e-10
+    assert np.linalg.norm(A @ v - e * v) < 1e-7
+
+
+def test_lanczos_invariant_subspace_small_problem():
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((4, 4))
+    A = A + A.T
+    e, v = O.lanczos_lowest(lambda x: A @ x, np.ones(4) + 0j, 8, 2)
+    assert abs(e - np.linalg.eigvalsh(A)[0]) < 1e-12
+
+
+def test_lanczos_matvec_count_matches_krylovkit_schedule():
+    rng = np.random.default_rng(2)
+    n = 200
+    A = np.diag(np.linspace(-1, 1, n)) + 0j
+    st = {}
+    O.lanczos_lowest(lambda x: A @ x, rng.standard_normal(n) + 0j, 3, 2, stats=st)
+    assert st["numops"] == 5        # 3 + (3 - keep=1)
+    st = {}
+    O.lanczos_lowest(lambda x: A @ x, rng.standard_normal(n) + 0j, 8, 2, stats=st)
+    assert st["numops"] == 12       # 8 + (8 - keep=4)
+
+
+def test_dmrg_tfim_free_fermion():
+    st = O.spinhalf()
+    N = 12
+    W = O.mpo_from_oplist(st, tfim(N))
+    psi = O.random_mps(2, N, 4, np.random.default_rng(1))
+    psi, E = O.dmrg(psi, W, maxdim=64, cutoff=1e-12, maxsweeps=12, minsweeps=12,
+                    numconverges=np.inf, krylovdim=8, kryloviter=2)
+    assert abs(np.real(E) - X.tfim_free_fermion_energy(N, 1.0, 0.5)) < 1e-9
+
+
+def test_dmrg_xxz_ed():
+    st = O.spinhalf()
+    N = 10
+    H = xxz(N)
+    W = O.mpo_from_oplist(st, H)
+    psi = O.random_mps(2, N, 8, np.random.default_rng(2))
+    psi, E = O.dmrg(psi, W, maxdim=64, cutoff=1e-12, maxsweeps=8, minsweeps=8,
+                    numconverges=np.inf)
+    E_ed = np.linalg.eigvalsh(X.oplist_to_dense(st, H))[0]
+    assert abs(np.real(E) - E_ed) < 1e-8
+    # energy of the returned state agrees with the Lanczos value
+    v = X.mps_to_dense(psi)
+    assert abs(X.dense_expect(v, X.oplist_to_dense(st, H)) - E_ed) < 1e-8
+
+
+def test_random_mps_is_normalised_and_canonical():
+    psi = O.random_mps(2, 8, 4, np.random.default_rng(3))
+    assert psi.center == 1
+    assert abs(np.linalg.norm(X.mps_to_dense(psi)) - 1) < 1e-12
+    assert psi.bonddims() == [1, 2, 4, 4, 4, 4, 4, 2, 1]
+
+
+def test_tebd_untruncated_matches_dense_gates():
+    st = O.spinhalf()
+    N = 8
+    H = xxz(N, 1.0, 0.5, lambda i: 0.2 * (-1) ** i)
+    psi = O.product_mps(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)])
+    v0 = X.mps_to_dense(psi)
+    rows = O.trotterize(st, H, 0.05, order=2, evol="real")
+    # the last gate of the even row is a one-site field gate
+    assert rows[1][1][-1].ndim == 2 and rows[1][0][-1] == N
+    zops = O.OpList(N)
+    for i in range(1, N + 1):
+        zops.add("z", i)
+    rec = {}
+    O.tebd(st, psi, H, 0.05, 0.25, 0.05, [zops], cutoff=0.0, maxdim=0, evol="real", record=rec)
+    v = v0
+    for _ in range(5):
+        v = X.apply_rows_dense(v, rows, N, 2)
+    v = v / np.linalg.norm(v)
+    z_dense = [X.dense_expect(v, X.oplist_to_dense(st, _single(N, "z", i))) for i in range(1, N + 1)]
+    assert np.allclose(np.real(rec["ops"][-1][0]), np.real(z_dense), atol=1e-10)
+    assert abs(abs(np.vdot(X.mps_to_dense(psi), v)) - 1) < 1e-10
+
+
+def _single(N, name, i):
+    o = O.OpList(N)
+    o.add(name, i)
+    return o
+
+
+def test_inner_matches_dense():
+    st = O.spinhalf()
+    N = 6
+    psi = O.random_mps(2, N, 3, np.random.default_rng(4))
+    ops = O.OpList(N)
+    ops.add("z", 2)
+    ops.add(["x", "y"], [3, 4], 0.7)
+    ops.add(["z", "x"], [1, 3], 1.3)
+    got = O.inner(st, psi, ops, psi)
+    v = X.mps_to_dense(psi)
+    for k in range(3):
+        one = O.OpList(N)
+        one.add(ops.ops[k], ops.sites[k], ops.coeffs[k])
+        assert abs(got[k] - np.vdot(v, X.oplist_to_dense(st, one) @ v)) < 1e-12
+
+
+def test_qjmc_single_site_decay_closed_form():
+    """H = 0, L = sqrt(g) s-: from |up>, no-jump evolution keeps |up> and the
+    jump probability per step is 1 - exp(-g dt) exactly."""
+    st = O.spinhalf()
+    N, g, dt = 1, 0.3, 0.01
+    H = O.OpList(N)
+    H.add("z", 1, 0.0)
+    L = O.OpList(N)
+    L.add("s-", 1, np.sqrt(g))
+    psi = O.product_mps(st, ["up"])
+    # draws: step1 (unused, decision=0.5 -> no jump), step2 (unused, 0.9999 -> jump, pick 0.1)
+    draws = [0.3, 0.5, 0.3, 0.9999, 0.1, 0.2, 0.5]
+    stream = O.algorithms.UniformStream(draws)
+    jumps, times = O.qjmc_simulation(st, psi, H, L, 3 * dt, dt, stream, cutoff=1e-12)
+    assert jumps == [1] and abs(times[0] - 2 * dt) < 1e-15
+    assert np.allclose(np.abs(psi[1].ravel()), [0, 1])
+
+
+def test_qjmc_matches_lindblad():
+    st = O.spinhalf()
+    N, dt, T = 2, 0.02, 0.6
+    H = O.OpList(N)
+    H.add(["z", "z"], [1, 2], 1.0)
+    H.add("x", 1, 0.8)
+    H.add("x", 2, 0.8)
+    L = O.OpList(N)
+    for i in (1, 2):
+        L.add("s-", i, np.sqrt(0.5))
+    zops = O.OpList(N)
+    zops.add("z", 1)
+    zops.add("z", 2)
+    rng = np.random.default_rng(7)
+    ntraj = 150
+    zs = []
+    for _ in range(ntraj):
+        psi = O.product_mps(st, ["up", "up"])
+        rec = {}
+        O.qjmc_simulation(st, psi, H, L, T, dt, lambda: float(rng.random()), [zops],
+                          save=T, cutoff=1e-12, record=rec)
+        zs.append(np.real(rec["ops"][-1][0]))
+    zs = np.array(zs)
+    Hd = X.oplist_to_dense(st, H)
+    Ls = [X.oplist_to_dense(st, _single(N, "s-", i)) * np.sqrt(0.5) for i in (1, 2)]
+    v0 = np.zeros(4, dtype=complex)
+    v0[0] = 1
+    rho = X.lindblad_evolve(Hd, Ls, np.outer(v0, v0.conj()), [T])[0]
+    for i in (1, 2):
+        ex = np.real(np.trace(rho @ X.oplist_to_dense(st, _single(N, "z", i))))
+        err = zs[:, i - 1].std() / np.sqrt(ntraj)
+        assert abs(zs[:, i - 1].mean() - ex) < 4 * err + 0.03
