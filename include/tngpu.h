@@ -1,0 +1,191 @@
+/*
+ * tngpu.h — C ABI of libtngpu.so, the GB300 (sm_103a) implementation of the
+ * finite-MPS hot path of TensorNetworks.jl (two-site DMRG, TEBD gate
+ * application, quantum-jump Monte Carlo).
+ *
+ * Conventions (the reference's, structures/mps/*.jl):
+ *   - every tensor is complex double, passed as interleaved (re, im) pairs in
+ *     column-major (Julia) order;
+ *   - MPS site  A[Dl, d, Dr]            (structures/mps/gmps.jl:8-13)
+ *   - MPO site  W[wl, d_out, d_in, wr]  (structures/mps/mpo.jl:6-12)
+ *   - gate      G[o1, i1, o2, i2] for two sites, G[o, i] for one site
+ *                                       (structures/mps/oplist.jl:134-156)
+ *   - sites and orthogonality centres are 1-based; centre 0 means "unset"
+ *     (structures/mps/abstractmps.jl:43-48).
+ *
+ * Every entry point returns an int32 status: TN_OK (0) or a negative code.
+ * tn_last_error() gives the message of the last failure on a context.  Host
+ * arrays are caller-owned and copied synchronously; handles own their device
+ * memory.  A context is used by one host thread at a time and owns one CUDA
+ * stream; every call has completed on the device when it returns.
+ */
+#ifndef TNGPU_H
+#define TNGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TN_OK                 0
+#define TN_ERR_INVALID       -1  /* bad argument (the reference's error("...")) */
+#define TN_ERR_CUDA          -2  /* CUDA runtime / library failure             */
+#define TN_ERR_OOM           -3  /* device allocation failed                   */
+#define TN_ERR_TIMEOUT       -4  /* a bounded device wait ran out              */
+#define TN_ERR_NUMERIC       -5  /* eigensolver / decomposition failure        */
+
+#define TN_PREC_FP64   0   /* plain FP64 (parity mode)                          */
+#define TN_PREC_MIXED  1   /* 3xTF32 tcgen05 products, FP64 Lanczos/truncation */
+
+typedef struct tn_ctx tn_ctx;
+typedef struct tn_mps tn_mps;     /* GMPS of rank 1 on the device */
+typedef struct tn_mpo tn_mpo;     /* GMPS of rank 2 on the device */
+typedef struct tn_gates tn_gates; /* GateList on the device       */
+
+/* Truncation keywords of svd(x, idx; cutoff, maxdim, mindim) (src/tensors.jl:168-215). */
+typedef struct tn_trunc_opts {
+    double cutoff;   /* 0 = no cutoff          */
+    int64_t maxdim;  /* 0 = no cap             */
+    int64_t mindim;  /* default 1              */
+} tn_trunc_opts;
+
+/* Keywords of dmrg (src/algorithms/mps/dmrg.jl:3-19). */
+typedef struct tn_dmrg_opts {
+    int32_t nsites;        /* must be 2                                   */
+    int32_t krylovdim;     /* default 3                                   */
+    int32_t kryloviter;    /* default 2                                   */
+    int32_t minsweeps;     /* default 1                                   */
+    int32_t maxsweeps;     /* default 1000; 0 = unlimited                 */
+    double tol;            /* default 1e-10                               */
+    double tolgrad;        /* default 1e-5                                */
+    double numconverges;   /* default 4 (Inf disables early stopping)     */
+    double cutoff;         /* default 1e-12                               */
+    int64_t maxdim;        /* default 1000                                */
+    int64_t mindim;        /* default 1                                   */
+    int32_t precision;     /* TN_PREC_FP64 or TN_PREC_MIXED               */
+    int32_t verbose;       /* print the reference's per-sweep line        */
+    int32_t max_bond_updates; /* 0 = run the sweeps; n > 0 = stop after n bond
+                                 optimisations (a bounded timing sample)  */
+} tn_dmrg_opts;
+
+typedef struct tn_dmrg_stats {
+    int32_t sweeps;
+    int32_t maxbonddim;
+    int64_t matvecs;
+    double seconds;
+    double energy_fp64;    /* FP64 <psi|H|psi> at the final centre (mixed mode) */
+    double last_discarded; /* discarded weight of the last truncation */
+    /* optional caller-owned per-sweep records (NULL to skip), capacity sweep_cap:
+     * device-timeline seconds between CUDA events recorded at sweep boundaries
+     * on the context's stream, the sweep's final local energy and max bond dim */
+    int32_t sweep_cap;
+    double* sweep_seconds;
+    double* sweep_energies;
+    int32_t* sweep_maxdim;
+    int32_t bond_updates;  /* bond optimisations performed */
+} tn_dmrg_stats;
+
+/* ---- context -------------------------------------------------------------- */
+int32_t tn_ctx_create(int32_t device, tn_ctx** out);
+int32_t tn_ctx_destroy(tn_ctx* ctx);
+const char* tn_last_error(tn_ctx* ctx);
+int32_t tn_version(void);
+/* Number of kernels this library launched on ctx since creation. */
+int64_t tn_kernel_launches(tn_ctx* ctx);
+
+/* ---- MPS / MPO handles (structures/mps/gmps.jl:8-21, mps.jl:6-12, mpo.jl:6-12) */
+/* bonddims has N+1 entries (bonddims[0] = bonddims[N] = 1 for a finite MPS);
+ * site_ptrs[i] points at the interleaved tensor [bonddims[i], d, bonddims[i+1]]. */
+int32_t tn_mps_upload(tn_ctx* ctx, int32_t N, int32_t d, const int64_t* bonddims,
+                      const double* const* site_ptrs, int32_t center, tn_mps** out);
+int32_t tn_mps_download(tn_ctx* ctx, const tn_mps* mps, double* const* site_ptrs);
+int32_t tn_mps_bonddims(tn_ctx* ctx, const tn_mps* mps, int64_t* bonddims, int32_t* center);
+int32_t tn_mps_copy(tn_ctx* ctx, const tn_mps* src, tn_mps** out);
+int32_t tn_mps_destroy(tn_mps* mps);
+/* wdims has N+1 entries; site_ptrs[i] is [wdims[i], d, d, wdims[i+1]]. */
+int32_t tn_mpo_upload(tn_ctx* ctx, int32_t N, int32_t d, const int64_t* wdims,
+                      const double* const* site_ptrs, tn_mpo** out);
+int32_t tn_mpo_destroy(tn_mpo* mpo);
+
+/* ---- gauge, norm, entropy (structures/mps/gmps.jl:29-112,184-189) -------- */
+int32_t tn_mps_movecenter(tn_ctx* ctx, tn_mps* mps, int32_t site, const tn_trunc_opts* trunc);
+int32_t tn_mps_norm(tn_ctx* ctx, tn_mps* mps, double* out_re_im);
+int32_t tn_mps_normalize(tn_ctx* ctx, tn_mps* mps);
+int32_t tn_mps_entropy(tn_ctx* ctx, tn_mps* mps, int32_t site, double* out);
+/* Singular values across bond (site, site+1) after movecenter!(site); *n in:
+ * capacity, out: count. */
+int32_t tn_mps_singular_values(tn_ctx* ctx, tn_mps* mps, int32_t site, double* out, int64_t* n);
+/* A <- op A on one site, op a d x d matrix (structures/mps/mps.jl:141-151). */
+int32_t tn_mps_applyop(tn_ctx* ctx, tn_mps* mps, int32_t site, const double* op);
+
+/* ---- expectation values (structures/mps/mps.jl:87-134) -------------------- */
+/* Per-term <bra|term|ket>.  Term t covers sites term_first[t] .. +term_len[t]-1;
+ * term_ops holds, term after term, term_len[t] interleaved d x d matrices (one
+ * per covered site; identity where the term has no operator); coeffs are
+ * complex (re, im).  out gets ntermsx(re, im). */
+int32_t tn_inner_terms(tn_ctx* ctx, const tn_mps* bra, const tn_mps* ket, int32_t nterms,
+                       const int32_t* term_first, const int32_t* term_len,
+                       const double* term_ops, const double* coeffs, double* out);
+
+/* ---- DMRG (src/algorithms/mps/dmrg.jl:1-154) ------------------------------ */
+int32_t tn_dmrg(tn_ctx* ctx, tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts* opts,
+                double* energy, tn_dmrg_stats* stats);
+
+/* ---- gates (structures/mps/gatelist.jl) ----------------------------------- */
+/* nrows rows; row r has row_len[r] gates; sites/gate_nsites/gate_ptrs list all
+ * gates row after row.  gate_ptrs[g] is [o1,i1,o2,i2] (2 sites) or [o,i]. */
+int32_t tn_gates_upload(tn_ctx* ctx, int32_t N, int32_t d, int32_t nrows, const int32_t* row_len,
+                        const int32_t* sites, const int32_t* gate_nsites,
+                        const double* const* gate_ptrs, tn_gates** out);
+int32_t tn_gates_destroy(tn_gates* gates);
+/* applygates! (gatelist.jl:191-227). */
+int32_t tn_applygates(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, const tn_trunc_opts* trunc);
+/* nsteps x (applygates!, lognorm += log(norm), normalize!) (tebd.jl:61-84). */
+int32_t tn_tebd_steps(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nsteps,
+                      const tn_trunc_opts* trunc, double* lognorm_accum);
+
+/* ---- QJMC (src/algorithms/mps/qjmc.jl) ------------------------------------ */
+/* Emission rates |c_j^2 <psi|L_j^dag L_j|psi>| of single-site jump operators
+ * (qjmc.jl:170-220); ops are d x d interleaved, coeffs complex. */
+int32_t tn_qjmc_rates(tn_ctx* ctx, tn_mps* psi, int32_t njump, const int32_t* sites,
+                      const double* ops, const double* coeffs, double* rates);
+/* One trajectory of qjmc_simulation with classical=true (qjmc.jl:28-166).
+ * draws: the uniform stream, consumed in the reference's order (one unused
+ * draw per step, one for the jump decision, one more on a jump).
+ * Observables (single-site ops) are evaluated at t=0 and every save_every
+ * steps into obs_out[(nsave_rows) x nobs] (re, im).  Jump indices are
+ * 1-based.  *njumps in: capacity, out: count; *ndraws_used out. */
+int32_t tn_qjmc_run(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t njump,
+                    const int32_t* jump_sites, const double* jump_ops, const double* jump_coeffs,
+                    int32_t nsteps, double dt, const double* draws, int64_t ndraws,
+                    const tn_trunc_opts* trunc, int32_t save_every, int32_t nobs,
+                    const int32_t* obs_sites, const double* obs_ops, double* obs_out,
+                    int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used);
+
+/* ---- unit-level kernels on host buffers (for parity tests) --------------- */
+/* out[a,s1',s2',c'] = sum L[a,w,b] W1[w,s1',s1,w'] W2[w',s2',s2,w''] th[b,s1,s2,c] R[c',w'',c]
+ * (structures/mps/projmps.jl:103-145). */
+int32_t tn_heff2_apply(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl, int64_t wm,
+                       int64_t wr, const double* L, const double* W1, const double* W2,
+                       const double* R, const double* theta, double* out, int32_t precision);
+/* L'[a',w',b'] = sum L[a,w,b] conj(A[a,s',a']) W[w,s',s,w'] A[b,s,b'] (projmps.jl:50-66). */
+int32_t tn_env_left(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl, int64_t wr,
+                    const double* L, const double* A, const double* W, double* out, int32_t precision);
+/* R[a,w,b] = sum A[b,s,b'] R'[a',w',b'] W[w,s',s,w'] conj(A[a,s',a']) (projmps.jl:74-95). */
+int32_t tn_env_right(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl, int64_t wr,
+                     const double* R, const double* A, const double* W, double* out, int32_t precision);
+/* Theta'[Dl,o1,o2,Dr] = sum G[o1,i1,o2,i2] A1[Dl,i1,k] A2[k,i2,Dr] (gatelist.jl:137-154). */
+int32_t tn_gate2_apply(tn_ctx* ctx, int64_t chil, int64_t chim, int64_t chir, int32_t d,
+                       const double* A1, const double* A2, const double* G, double* out);
+/* Truncated split of theta[m x n] (tensors.jl:168-227 keep rule).  direction 0:
+ * X isometric, Y = S Vt; direction 1: X = U S, Y co-isometric.  X gets m x k,
+ * Y k x n, S the k kept singular values; *k in: capacity, out: kept count. */
+int32_t tn_truncate(tn_ctx* ctx, int64_t m, int64_t n, const double* theta,
+                    const tn_trunc_opts* trunc, int32_t direction, double* X, double* Y,
+                    double* S, int64_t* k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TNGPU_H */

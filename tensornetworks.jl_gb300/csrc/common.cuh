@@ -1,0 +1,159 @@
+// Internal declarations shared by the libtngpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tngpu.h"
+
+typedef double2 cplx;
+
+namespace tn {
+
+// Error carrying a TN_ERR_* status; caught at the C ABI boundary.
+struct Error : public std::runtime_error {
+    int32_t code;
+    Error(int32_t c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define TN_CHECK_CUDA(expr)                                                          \
+    do {                                                                             \
+        cudaError_t _e = (expr);                                                     \
+        if (_e != cudaSuccess)                                                       \
+            throw ::tn::Error(_e == cudaErrorMemoryAllocation ? TN_ERR_OOM : TN_ERR_CUDA, \
+                              std::string(#expr) + ": " + cudaGetErrorString(_e));   \
+    } while (0)
+
+#define TN_CHECK_SOLVER(expr)                                                        \
+    do {                                                                             \
+        cusolverStatus_t _s = (expr);                                                \
+        if (_s != CUSOLVER_STATUS_SUCCESS)                                           \
+            throw ::tn::Error(TN_ERR_CUDA, std::string(#expr) + ": cusolver status " + \
+                              std::to_string((int)_s));                             \
+    } while (0)
+
+#define TN_REQUIRE(cond, msg)                                                        \
+    do {                                                                             \
+        if (!(cond)) throw ::tn::Error(TN_ERR_INVALID, msg);                         \
+    } while (0)
+
+// Stream-ordered device buffer drawn from the context's memory pool.
+struct Ctx;
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    Ctx* ctx = nullptr;
+    DBuf() = default;
+    DBuf(Ctx* c, size_t b);
+    ~DBuf();
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+    DBuf& operator=(DBuf&& o) noexcept;
+    void reset();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+    cplx* c() const { return static_cast<cplx*>(p); }
+    double* d() const { return static_cast<double*>(p); }
+};
+
+// Growable scratch buffer (keeps its allocation between uses).
+struct Scratch {
+    DBuf buf;
+    void* get(Ctx* ctx, size_t bytes);
+    cplx* c(Ctx* ctx, size_t n) { return static_cast<cplx*>(get(ctx, n * sizeof(cplx))); }
+    double* d(Ctx* ctx, size_t n) { return static_cast<double*>(get(ctx, n * sizeof(double))); }
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    int sm_count = 0;
+    // reusable scratch for the hot path
+    Scratch s_gram, s_eigval, s_work, s_x, s_y, s_t1, s_t2, s_dot, s_coef, s_mixa, s_mixb, s_mixc,
+        s_mixd, s_mixe, s_mixf;
+    int* d_info = nullptr;
+    double* h_pinned = nullptr;  // small pinned staging area
+    size_t h_pinned_n = 0;
+    void sync() { TN_CHECK_CUDA(cudaStreamSynchronize(stream)); }
+    void count() { ++launches; }
+    double* pinned(size_t n);
+};
+
+// ---- small complex helpers ----------------------------------------------
+__host__ __device__ inline cplx cmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ inline cplx cadd(cplx a, cplx b) { return cmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline cplx csub(cplx a, cplx b) { return cmk(a.x - b.x, a.y - b.y); }
+__host__ __device__ inline cplx cmul(cplx a, cplx b) {
+    return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline cplx cconj(cplx a) { return cmk(a.x, -a.y); }
+__host__ __device__ inline cplx cfma(cplx a, cplx b, cplx c) {  // a*b + c
+    return cmk(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+
+// ---- kernels (kernels_fp64.cu) -----------------------------------------
+enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };  // R: conjugate without transpose
+
+// C[m x n] = alpha * op(A) * op(B) + beta * C, column-major, batched by count.
+void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha, const cplx* A,
+           int64_t lda, int64_t strideA, const cplx* B, int64_t ldb, int64_t strideB, cplx beta,
+           cplx* C, int64_t ldc, int64_t strideC, int64_t batch = 1);
+
+// out[a + lda_o*J + ldc_o*c] (=|+=) sum_I in[a + lda_i*I + ldc_i*c] * M[I + nI*J]
+void small_apply(Ctx* ctx, const cplx* in, cplx* out, const cplx* M, int nI, int nJ, int64_t na,
+                 int64_t nc, int64_t lda_i, int64_t ldc_i, int64_t lda_o, int64_t ldc_o,
+                 bool accumulate = false);
+
+// out[j] = <v_j, w> for K vectors; result left in device memory dout (K cplx).
+void multi_dot(Ctx* ctx, const cplx* const* dV, int K, const cplx* w, int64_t n, cplx* dout);
+// w += sum_j coef[j] * v_j, coef on the device (K cplx); sign applied to coefs.
+void multi_axpy(Ctx* ctx, cplx* w, const cplx* const* dV, const cplx* dcoef, int K, int64_t n,
+                double sign);
+void zscale(Ctx* ctx, cplx* x, int64_t n, cplx a);
+void zscale_dev(Ctx* ctx, cplx* x, int64_t n, const double* dnorm, int invert);  // x *= 1/norm
+void zcopy(Ctx* ctx, cplx* dst, const cplx* src, int64_t n);
+void zfill(Ctx* ctx, cplx* dst, int64_t n, cplx v);
+void bilinear_dot(Ctx* ctx, const cplx* x, const cplx* y, int64_t n, cplx* dout);  // sum x*y
+double znorm2(Ctx* ctx, const cplx* x, int64_t n);  // ||x||^2, synchronous
+// take k eigenvectors, largest first: dst[:, j] = G[:, n-1-j]
+void take_top_eigvecs(Ctx* ctx, const cplx* G, int64_t n, int64_t k, cplx* dst);
+// scale columns: X[:, j] *= s[j] (s real, device)
+// dst (c x r) = src(r x c)^H, tiled through shared memory for coalescing
+void conj_transpose(Ctx* ctx, const cplx* src, int64_t r, int64_t c, cplx* dst);
+void scale_cols(Ctx* ctx, cplx* X, int64_t m, int64_t k, const double* s, int invert);
+// column norms of X (m x k) / row norms of Y (k x n), warp-shuffle reductions
+void col_norms(Ctx* ctx, const cplx* X, int64_t m, int64_t k, double* out);
+void row_norms(Ctx* ctx, const cplx* Y, int64_t k, int64_t n, double* out);
+void scale_rows(Ctx* ctx, cplx* X, int64_t k, int64_t n, const double* s, int invert);
+
+// Keep rule of tensors.jl:200-215 on ascending eigenvalues lam[0..n) of a Gram
+// matrix whose top sz values are the squared singular values.  Writes
+// (k, total, discarded) to host.  Also writes kept singular values (descending)
+// into dS when non-null.
+struct KeepResult { int64_t k; double total; double discarded; };
+KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double cutoff,
+                     int64_t maxdim, int64_t mindim, double* dS);
+
+// ---- linear algebra (linalg.cu) ----------------------------------------
+// Truncated split theta (m x n) ~= X (m x k) Y (k x n).  left_iso: X is an
+// isometry (sweeping right); else Y is a co-isometry (sweeping left).  X, Y
+// are allocated into the given DBufs.  Singular values (descending) go to S
+// (host vector) when non-null.
+struct SplitResult { int64_t k; double discarded; double total; };
+SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, double cutoff,
+                        int64_t maxdim, int64_t mindim, bool left_iso, DBuf& X, DBuf& Y,
+                        std::vector<double>* S);
+// Hermitian eigen-decomposition in place (eigenvectors overwrite G), ascending.
+void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam);
+
+}  // namespace tn

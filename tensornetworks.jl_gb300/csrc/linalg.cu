@@ -1,0 +1,131 @@
+// Context, stream-ordered memory, and the truncated two-factor split that
+// replaces LAPACK gesdd in svd(x, idx; cutoff, maxdim, mindim)
+// (src/tensors.jl:168-227).
+//
+// The split forms the Gram matrix on the side of the isometric factor, so the
+// isometry is an eigenvector matrix (orthonormal to working precision) and
+// the other factor is a projection; no division by small singular values is
+// needed.  The Gram product runs on our GEMM, the Hermitian eigenproblem on
+// cuSOLVER's zheevd (FP64), and the keep rule on the warp-shuffle kernel.
+#include "common.cuh"
+
+#include <cstring>
+
+namespace tn {
+
+// ---- memory ----------------------------------------------------------------
+DBuf::DBuf(Ctx* c, size_t b) : ctx(c), bytes(b) {
+    if (b == 0) return;
+    cudaError_t e = cudaMallocAsync(&p, b, c->stream);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        bytes = 0;
+        (void)cudaGetLastError();
+        throw Error(TN_ERR_OOM, "device allocation of " + std::to_string(b) + " bytes failed");
+    }
+}
+DBuf::~DBuf() { reset(); }
+DBuf& DBuf::operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+        reset();
+        p = o.p;
+        bytes = o.bytes;
+        ctx = o.ctx;
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    return *this;
+}
+void DBuf::reset() {
+    if (p && ctx) cudaFreeAsync(p, ctx->stream);
+    p = nullptr;
+    bytes = 0;
+}
+
+void* Scratch::get(Ctx* ctx, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (buf.bytes < bytes) {
+        buf.reset();
+        buf = DBuf(ctx, bytes + bytes / 4);
+    }
+    return buf.p;
+}
+
+double* Ctx::pinned(size_t n) {
+    if (h_pinned_n < n) {
+        if (h_pinned) cudaFreeHost(h_pinned);
+        h_pinned = nullptr;
+        TN_CHECK_CUDA(cudaMallocHost(&h_pinned, n * sizeof(double)));
+        h_pinned_n = n;
+    }
+    return h_pinned;
+}
+
+// ---- eigen-decomposition ---------------------------------------------------
+void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam) {
+    int lwork = 0;
+    TN_CHECK_SOLVER(cusolverDnZheevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                                CUBLAS_FILL_MODE_LOWER, (int)n,
+                                                reinterpret_cast<cuDoubleComplex*>(G), (int)n,
+                                                dlam, &lwork));
+    cuDoubleComplex* work = static_cast<cuDoubleComplex*>(
+        ctx->s_work.get(ctx, sizeof(cuDoubleComplex) * (size_t)std::max(lwork, 1)));
+    TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                     (int)n, reinterpret_cast<cuDoubleComplex*>(G), (int)n, dlam,
+                                     work, lwork, ctx->d_info));
+    ctx->count();
+    int info = 0;
+    TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (info != 0) throw Error(TN_ERR_NUMERIC, "zheevd failed, info = " + std::to_string(info));
+}
+
+// ---- truncated split -------------------------------------------------------
+SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, double cutoff,
+                        int64_t maxdim, int64_t mindim, bool left_iso, DBuf& X, DBuf& Y,
+                        std::vector<double>* S) {
+    TN_REQUIRE(m > 0 && n > 0, "trunc_split: empty matrix");
+    const int64_t sz = std::min(m, n);
+    const int64_t g = left_iso ? m : n;
+    TN_REQUIRE(g <= 46340, "trunc_split: Gram matrix too large for 32-bit solver indexing");
+    cplx* G = ctx->s_gram.c(ctx, (size_t)g * g);
+    double* lam = ctx->s_eigval.d(ctx, (size_t)g + sz);
+    double* dS = lam + g;
+    const cplx one = cmk(1, 0), zero = cmk(0, 0);
+    if (left_iso)  // G = theta theta^H
+        zgemm(ctx, OP_N, OP_C, m, m, n, one, theta, m, 0, theta, m, 0, zero, G, m, 0);
+    else  // G = theta^H theta
+        zgemm(ctx, OP_C, OP_N, n, n, m, one, theta, m, 0, theta, m, 0, zero, G, n, 0);
+    heevd(ctx, G, g, lam);
+    KeepResult kr = keep_rule(ctx, lam, g, sz, cutoff, maxdim, mindim, dS);
+    const int64_t k = kr.k;
+    if (left_iso) {
+        X = DBuf(ctx, sizeof(cplx) * m * k);
+        Y = DBuf(ctx, sizeof(cplx) * k * n);
+        take_top_eigvecs(ctx, G, m, k, X.c());
+        zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
+    } else {
+        DBuf V(ctx, sizeof(cplx) * n * k);
+        take_top_eigvecs(ctx, G, n, k, V.c());
+        X = DBuf(ctx, sizeof(cplx) * m * k);
+        Y = DBuf(ctx, sizeof(cplx) * k * n);
+        zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V.c(), n, 0, zero, X.c(), m, 0);
+        conj_transpose(ctx, V.c(), n, k, Y.c());  // Y = V^H (k x n)
+    }
+    if (S) {
+        // Singular values as norms of the projected factor (U^H theta rows or
+        // theta V columns): accurate to eps * sigma_max even where the Gram
+        // eigenvalue sits at the sqrt(eps) noise floor.
+        if (left_iso)
+            row_norms(ctx, Y.c(), k, n, dS);
+        else
+            col_norms(ctx, X.c(), m, k, dS);
+        S->resize(k);
+        TN_CHECK_CUDA(cudaMemcpyAsync(S->data(), dS, sizeof(double) * k, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        ctx->sync();
+    }
+    return SplitResult{k, kr.discarded, kr.total};
+}
+
+}  // namespace tn

@@ -1,0 +1,16 @@
+"""tngpu: the finite-MPS hot path of TensorNetworks.jl on GB300.
+
+The names mirror the reference's exports (src/exports.jl): ``spinhalf``,
+``OpList``, ``MPO``, ``randomMPS``, ``productMPS``, ``dmrg``,
+``trotterize``, ``applygates``, ``tebd``, ``qjmc_simulation``, ``inner``,
+observers.  Every contraction, truncation and eigensolve runs in
+``libtngpu.so`` on the GPU; nothing here computes on the CPU beyond building
+model inputs (operator tables, MPO tensors, 4x4 gate exponentials).
+"""
+
+from ._lib import Context, TNError, context, load  # noqa: F401
+from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEBDEnergy,  # noqa: F401
+                         TEBDNorm, TEBDOperators, applygates, dmrg, qjmc_gates,
+                         qjmc_simulation, tebd, trotterize)
+from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
+from .mps import GMPS, MPO, MPOHandle, entropy, inner, productMPS, randomMPS  # noqa: F401

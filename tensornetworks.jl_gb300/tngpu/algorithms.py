@@ -1,0 +1,356 @@
+"""dmrg, trotterize/applygates!, tebd and qjmc_simulation with the reference's
+arguments, keywords, return values and observers
+(src/algorithms/mps/{dmrg,tebd,qjmc}.jl, structures/mps/gatelist.jl).
+
+Each call hands whole algorithm stages to libtngpu.so; the host loop only
+sequences steps and records observers.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .models import OpList, trotter_rows
+from .mps import GMPS, MPOHandle, inner
+
+
+# ---------------------------------------------------------------------------
+# DMRG (dmrg.jl:1-154)
+# ---------------------------------------------------------------------------
+def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
+         maxsweeps=1000, tol=1e-10, tolgrad=1e-5, numconverges=4, cutoff=1e-12, maxdim=1000,
+         mindim=1, verbose=True, precision="fp64", stats=None, max_bond_updates=0):
+    """Two-site DMRG; mutates ``psi`` and returns (psi, energy).
+
+    ``stats`` (a dict) receives sweeps, matvecs, per-sweep device seconds and
+    energies; ``max_bond_updates`` > 0 stops after that many bond
+    optimisations (a bounded timing sample)."""
+    if psi.rank != 1:
+        raise ValueError("Psi must be a GMPS of rank 1 (vector).")
+    if len(H) != len(psi) or H.dim != psi.dim:
+        raise ValueError("GMPS must share the same properties.")
+    if nsites != 2:
+        raise ValueError("only two-site DMRG (nsites=2) is on this path")
+    o = L.DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
+                   float(numconverges), cutoff, maxdim, mindim, L.PREC[precision], int(bool(verbose)),
+                   int(max_bond_updates))
+    e = C.c_double()
+    st = L.DmrgStats()
+    cap = maxsweeps if maxsweeps > 0 else 1000
+    secs, ens = np.zeros(cap), np.zeros(cap)
+    mds = np.zeros(cap, dtype=np.int32)
+    st.sweep_cap = cap
+    st.sweep_seconds, st.sweep_energies = L.as_dp(secs), L.as_dp(ens)
+    st.sweep_maxdim = mds.ctypes.data_as(L.i32p)
+    ctx = psi.ctx
+    ctx.check(ctx.lib.tn_dmrg(ctx.h, psi._h, H._h, C.byref(o), C.byref(e), C.byref(st)))
+    if stats is not None:
+        stats.update(sweeps=st.sweeps, maxbonddim=st.maxbonddim, matvecs=st.matvecs,
+                     seconds=st.seconds, energy_fp64=st.energy_fp64,
+                     last_discarded=st.last_discarded, bond_updates=st.bond_updates,
+                     sweep_seconds=secs[: min(st.sweeps, cap)].tolist(),
+                     sweep_energies=ens[: min(st.sweeps, cap)].tolist(),
+                     sweep_maxdim=mds[: min(st.sweeps, cap)].tolist())
+    return psi, e.value
+
+
+# ---------------------------------------------------------------------------
+# Gates (gatelist.jl)
+# ---------------------------------------------------------------------------
+class GateList:
+    """Rows of non-overlapping gates uploaded to the GPU (gatelist.jl:8-62)."""
+
+    def __init__(self, length, rows, dim, ctx=None):
+        self.length = length
+        self.rows = rows
+        self.ctx = ctx or L.context()
+        row_len = np.asarray([len(s) for s, _ in rows], dtype=np.int32)
+        sites = np.asarray([s for ss, _ in rows for s in ss], dtype=np.int32)
+        nsites = np.asarray([g.ndim // 2 for _, gs in rows for g in gs], dtype=np.int32)
+        mats = [L.cplx_f(g) for _, gs in rows for g in gs]
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.tn_gates_upload(
+            self.ctx.h, length, dim, len(rows), row_len.ctypes.data_as(L.i32p),
+            sites.ctypes.data_as(L.i32p), nsites.ctypes.data_as(L.i32p), L.ptr_array(mats),
+            C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self.ctx.lib.tn_gates_destroy(h)
+            self._h = None
+
+
+def trotterize(st, ops: OpList, dt, order=2, evol="imag", ctx=None):
+    """gatelist.jl:75-121"""
+    return GateList(ops.length, trotter_rows(st, ops, dt, order, evol), st.dim, ctx)
+
+
+def applygates(psi: GMPS, gates: GateList, cutoff=0.0, maxdim=0, mindim=1):
+    """applygates! (gatelist.jl:191-227)"""
+    t = L.trunc(cutoff, maxdim, mindim)
+    psi.ctx.check(psi.ctx.lib.tn_applygates(psi.ctx.h, psi._h, gates._h, C.byref(t)))
+
+
+applygates_ = applygates
+
+
+# ---------------------------------------------------------------------------
+# TEBD (tebd.jl:3-219)
+# ---------------------------------------------------------------------------
+class TEBDObserver:
+    def measure(self, time, psi, norm, energy):
+        return True
+
+    def checkdone(self):
+        return False
+
+
+class TEBDNorm(TEBDObserver):
+    """tebd.jl:132-159"""
+
+    def __init__(self, tol=1e-10):
+        self.times, self.measurements, self.tol = [], [], tol
+
+    def measure(self, time, psi, norm, energy):
+        self.times.append(time)
+        self.measurements.append(norm)
+
+    def checkdone(self):
+        if len(self.times) < 3:
+            return False
+        m, t = self.measurements, self.times
+        E1 = (m[-1] - m[-2]) / (t[-1] - t[-2])
+        E2 = (m[-2] - m[-3]) / (t[-2] - t[-3])
+        if abs(E2 + E1) < 1e-8:
+            return abs(E2 - E1) < self.tol
+        return abs((E2 - E1) / (0.5 * (E2 + E1))) < self.tol
+
+
+class TEBDEnergy(TEBDObserver):
+    """tebd.jl:168-193"""
+
+    def __init__(self, tol=1e-10):
+        self.times, self.measurements, self.tol = [], [], tol
+
+    def measure(self, time, psi, norm, energy):
+        self.times.append(time)
+        self.measurements.append(energy)
+
+    def checkdone(self):
+        if len(self.times) < 3:
+            return False
+        E1, E2 = self.measurements[-1], self.measurements[-2]
+        if 0.5 * abs(E2 + E1) < 1e-8:
+            return abs(E2 - E1) < self.tol
+        return abs(2 * (E2 - E1) / (E2 + E1)) < self.tol
+
+
+class TEBDOperators(TEBDObserver):
+    """tebd.jl:201-219"""
+
+    def __init__(self, st, oplist):
+        self.times, self.measurements, self.st, self.oplist = [], [], st, oplist
+
+    def measure(self, time, psi, norm, energy):
+        self.times.append(time)
+        self.measurements.append(inner(self.st, psi, self.oplist, psi))
+
+
+def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, maxdim=0,
+         mindim=1, evol="imag", order=2, norm=0.0, verbose=False):
+    """Time evolution without projectors (tebd.jl:3-100); returns (psi, energy)."""
+    if st.dim != psi.dim:
+        raise ValueError("Sitetypes and MPS physical dimensions do not match.")
+    if len(psi) != H.length:
+        raise ValueError("OpList and MPS have different lengths.")
+    if evol not in ("imag", "real"):
+        raise ValueError("evol must be real of imag.")
+    if order not in (1, 2):
+        raise ValueError("Only first or second order trotter supported.")
+    gates = trotterize(st, H, dt, order=order, evol=evol, ctx=psi.ctx)
+    nsteps = int(round(tmax / dt))
+    save = dt if save < dt else save
+    nsave = int(round(save / dt))
+    normal = float(norm)
+    energy = float(np.real(np.sum(inner(st, psi, H, psi))))
+    for ob in observers:
+        ob.measure(0.0, psi, normal, energy)
+    psi.norm()  # log(norm(psi)) at tebd.jl:61 canonicalises an unset centre
+    t = L.trunc(cutoff, maxdim, mindim)
+    step = 0
+    converged = False
+    while not converged:
+        ln = C.c_double(0.0)
+        psi.ctx.check(psi.ctx.lib.tn_tebd_steps(psi.ctx.h, psi._h, gates._h, 1, C.byref(t), C.byref(ln)))
+        normal += ln.value
+        step += 1
+        converged = step >= nsteps
+        if step % nsave == 0:
+            if verbose:
+                print(f"time={step * dt:.4f}, energy={energy:.12f}, maxbonddim={psi.maxbonddim()} ")
+            energy = float(np.real(np.sum(inner(st, psi, H, psi))))
+            for ob in observers:
+                ob.measure(step * dt, psi, normal, energy)
+                converged = converged or ob.checkdone()
+    return psi, energy
+
+
+# ---------------------------------------------------------------------------
+# QJMC (qjmc.jl:9-310)
+# ---------------------------------------------------------------------------
+def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
+    """Escape operators c^2 L^dag L and Heff = -iH - 1/2 sum escape (qjmc.jl:9-26)."""
+    esc = OpList(jumpops.length)
+    for ops, sites, c in zip(jumpops.ops, jumpops.sites, jumpops.coeffs):
+        esc.add([st.opprod([st.dag(o), o]) for o in ops], sites, c ** 2)
+    heff = (-1j) * H + (-0.5) * esc
+    return heff, trotter_rows(st, heff, dt, **kw)
+
+
+class QJMCOperators:
+    """qjmc.jl:238-260"""
+
+    def __init__(self, oplist, st, save=False, savefile=""):
+        self.times, self.measurements, self.oplist, self.st = [], [], oplist, st
+
+    def measure(self, time, psi, jumps, jumptimes):
+        self.times.append(time)
+        self.measurements.append(inner(self.st, psi, self.oplist, psi))
+
+
+class QJMCActivity:
+    """qjmc.jl:264-285 (HDF5 saving is outside this path)."""
+
+    def __init__(self, save=False, savefile=""):
+        self.time, self.jumps = 0.0, 0
+
+    def measure(self, time, psi, jumps, jumptimes):
+        self.time = time
+        self.jumps = len(jumps)
+
+
+class QJMCEntropy:
+    """qjmc.jl:293-310"""
+
+    def __init__(self):
+        self.times, self.measurements = [], []
+
+    def measure(self, time, psi, jumps, jumptimes):
+        self.times.append(time)
+        self.measurements.append([psi.entropy(i) for i in range(1, len(psi))])
+
+
+def qjmc_simulation(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, observers=(), save=0.0,
+                    cutoff=1e-12, mindim=1, maxdim=0, classical=True, verbose=False, rand=None,
+                    draws=None):
+    """One trajectory (qjmc.jl:28-166); mutates ``psi`` and returns (jumps,
+    jumptimes) with 1-based jump indices.
+
+    Uniform draws come from ``draws`` (an explicit array consumed in the
+    reference's order) or ``rand`` (a numpy Generator).  Single-site jump
+    operators and single-site observables run the whole trajectory inside the
+    library; other observers are sampled from the host between steps."""
+    if not classical:
+        raise NotImplementedError("the norm-based (classical=false) branch is not on this path")
+    save = dt if save == 0 else save
+    steps = math.ceil(round(tmax / dt, 5))
+    savesteps = math.ceil(round(save / dt))
+    _, rows = qjmc_gates(st, H, jumpops, dt)
+    gates = GateList(H.length, rows, st.dim, psi.ctx)
+    if any(len(s) != 1 for s in jumpops.sites):
+        raise NotImplementedError("multi-site jump operators are not on this path")
+    if draws is None:
+        g = rand if rand is not None else np.random.default_rng()
+        draws = g.random(3 * steps + 3)
+    draws = np.ascontiguousarray(draws, dtype=np.float64)
+    jsites = np.asarray([s[0] for s in jumpops.sites], dtype=np.int32)
+    jops = np.concatenate([L.cplx_f(st.op(o[0])).ravel(order="F") for o in jumpops.ops]).astype(np.complex128)
+    jco = np.asarray(jumpops.coeffs, dtype=np.complex128)
+    fast_obs = all(isinstance(o, QJMCOperators) and all(len(s) == 1 for s in o.oplist.sites)
+                   for o in observers)
+    ctx = psi.ctx
+    t = L.trunc(cutoff, maxdim, mindim)
+    cap = steps + 1
+    jumps = np.zeros(cap, dtype=np.int32)
+    jtimes = np.zeros(cap)
+    nj = C.c_int32(cap)
+    used = C.c_int64(0)
+    if fast_obs:
+        obs_sites, obs_ops, owner = [], [], []
+        for k, o in enumerate(observers):
+            for ops, sites, c in zip(o.oplist.ops, o.oplist.sites, o.oplist.coeffs):
+                obs_sites.append(sites[0])
+                obs_ops.append(complex(c) * st.op(ops[0]))
+                owner.append(k)
+        nobs = len(obs_sites)
+        nrows = steps // savesteps + 1
+        out = np.zeros((nrows, max(nobs, 1)), dtype=np.complex128)
+        osites = np.asarray(obs_sites or [1], dtype=np.int32)
+        oops = (np.concatenate([L.cplx_f(m).ravel(order="F") for m in obs_ops])
+                if nobs else np.zeros(4, dtype=np.complex128)).astype(np.complex128)
+        ctx.check(ctx.lib.tn_qjmc_run(
+            ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
+            L.as_dp(jco), steps, float(dt), L.as_dp(draws), draws.size, C.byref(t), savesteps,
+            nobs, osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
+            jumps.ctypes.data_as(L.i32p), L.as_dp(jtimes), C.byref(nj), C.byref(used)))
+        times = [0.0] + [dt * savesteps * (r + 1) for r in range(nrows - 1)]
+        # reproduce the reference's accumulated time values
+        tt, acc = 0.0, [0.0]
+        for i in range(1, steps + 1):
+            tt += dt
+            if i % savesteps == 0:
+                acc.append(tt)
+        times = acc
+        for k, o in enumerate(observers):
+            cols = [j for j, w in enumerate(owner) if w == k]
+            for r in range(nrows):
+                o.times.append(times[r])
+                o.measurements.append(out[r, cols].copy())
+        n = nj.value
+        return [int(x) for x in jumps[:n]], [float(x) for x in jtimes[:n]]
+    # host-sequenced trajectory for general observers
+    jl, jt = [], []
+    pos = 0
+
+    def nxt():
+        nonlocal pos
+        if pos >= draws.size:
+            raise IndexError("uniform draw stream exhausted")
+        pos += 1
+        return float(draws[pos - 1])
+
+    time = 0.0
+    for o in observers:
+        o.measure(time, psi, jl, jt)
+    rates = np.zeros(len(jsites))
+    N = len(psi)
+    for i in range(1, steps + 1):
+        applygates(psi, gates, cutoff, maxdim, mindim)
+        nxt()
+        psi.normalize()
+        ctx.check(ctx.lib.tn_qjmc_rates(ctx.h, psi._h, len(jsites), jsites.ctypes.data_as(L.i32p),
+                                        L.as_dp(jops), L.as_dp(jco), L.as_dp(rates)))
+        er = float(np.sum(rates))
+        if nxt() > math.exp(-er * dt):
+            r = nxt()
+            idx = int(np.nonzero(r < np.cumsum(rates) / er)[0][0])
+            psi.movecenter(1)
+            psi.applyop(st, jumpops.ops[idx], jumpops.sites[idx])
+            psi.movecenter(N)
+            psi.movecenter(1, cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+            psi.normalize()
+            jl.append(idx + 1)
+            jt.append(time + dt)
+        time += dt
+        if i % savesteps == 0:
+            if verbose:
+                print(f"time={time:.5f}, jumps={len(jl)}, maxbonddim={psi.maxbonddim()}")
+            for o in observers:
+                o.measure(time, psi, jl, jt)
+    return jl, jt

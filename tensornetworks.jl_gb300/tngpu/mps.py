@@ -1,0 +1,232 @@
+"""Device-resident GMPS and MPO handles with the reference's operations
+(structures/mps/gmps.jl, mps.jl, mpo.jl).  All arithmetic runs in
+libtngpu.so on the GPU; the host only holds handles and small inputs."""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .models import Sitetypes, mpo_tensors
+
+
+def _f(x, shape):
+    return np.reshape(x, shape, order="F")
+
+
+class GMPS:
+    """Rank-1 GMPS (an MPS) held on the GPU.  Sites and the orthogonality
+    centre are 1-based; centre 0 means unset (gmps.jl:8-13)."""
+
+    rank = 1
+
+    def __init__(self, handle, N, dim, ctx):
+        self._h = handle
+        self.N = N
+        self.dim = dim
+        self.ctx = ctx
+
+    # -- construction / transfer ------------------------------------------------
+    @classmethod
+    def from_tensors(cls, tensors, center=0, ctx=None):
+        ctx = ctx or L.context()
+        ts = [L.cplx_f(t) for t in tensors]
+        N = len(ts)
+        d = ts[0].shape[1]
+        dims = [ts[0].shape[0]] + [t.shape[2] for t in ts]
+        for i, t in enumerate(ts):
+            if t.ndim != 3 or t.shape[1] != d or t.shape[0] != dims[i] or t.shape[2] != dims[i + 1]:
+                raise ValueError("site tensors do not chain")
+        dims_arr = (C.c_int64 * (N + 1))(*dims)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.tn_mps_upload(ctx.h, N, d, dims_arr, L.ptr_array(ts), center, C.byref(h)))
+        return cls(h, N, d, ctx)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and self.ctx.h:
+            self.ctx.lib.tn_mps_destroy(h)
+            self._h = None
+
+    def __len__(self):
+        return self.N
+
+    def _query(self):
+        buf = (C.c_int64 * (self.N + 1))()
+        c = C.c_int32()
+        self.ctx.check(self.ctx.lib.tn_mps_bonddims(self.ctx.h, self._h, buf, C.byref(c)))
+        return [int(buf[i]) for i in range(self.N + 1)], int(c.value)
+
+    def bonddims(self):
+        """[1, chi_1, ..., chi_{N-1}, 1]"""
+        return self._query()[0]
+
+    @property
+    def center(self):
+        return self._query()[1]
+
+    def tensors(self):
+        """Download the site tensors as complex128 arrays [Dl, d, Dr]."""
+        dims = self.bonddims()
+        out = [np.zeros((dims[i], self.dim, dims[i + 1]), dtype=np.complex128, order="F")
+               for i in range(self.N)]
+        self.ctx.check(self.ctx.lib.tn_mps_download(self.ctx.h, self._h, L.ptr_array(out)))
+        return out
+
+    def __getitem__(self, i):
+        return self.tensors()[i - 1]
+
+    def copy(self):
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.tn_mps_copy(self.ctx.h, self._h, C.byref(h)))
+        return GMPS(h, self.N, self.dim, self.ctx)
+
+    deepcopy = copy
+
+    def maxbonddim(self):
+        """abstractmps.jl:75-81"""
+        return max([1] + self.bonddims()[1:-1])
+
+    # -- gauge / norm (gmps.jl:29-112) --------------------------------------------
+    def movecenter(self, idx, cutoff=0.0, maxdim=0, mindim=1):
+        t = L.trunc(cutoff, maxdim, mindim)
+        self.ctx.check(self.ctx.lib.tn_mps_movecenter(self.ctx.h, self._h, idx, C.byref(t)))
+
+    def norm(self):
+        out = (C.c_double * 2)()
+        self.ctx.check(self.ctx.lib.tn_mps_norm(self.ctx.h, self._h, out))
+        return complex(out[0], out[1])
+
+    def normalize(self):
+        self.ctx.check(self.ctx.lib.tn_mps_normalize(self.ctx.h, self._h))
+
+    def entropy(self, site):
+        """gmps.jl:184-189"""
+        out = C.c_double()
+        self.ctx.check(self.ctx.lib.tn_mps_entropy(self.ctx.h, self._h, site, C.byref(out)))
+        return out.value
+
+    def singular_values(self, site):
+        cap = max(self.bonddims()) * self.dim + 1
+        buf = np.zeros(cap)
+        n = C.c_int64(cap)
+        self.ctx.check(self.ctx.lib.tn_mps_singular_values(self.ctx.h, self._h, site, L.as_dp(buf),
+                                                           C.byref(n)))
+        return buf[: n.value].copy()
+
+    def applyop(self, st, ops, sites):
+        """applyop! (mps.jl:141-151): A <- O A, no coefficient."""
+        if isinstance(ops, str):
+            ops, sites = [ops], [sites]
+        for o, s in zip(ops, sites):
+            m = L.cplx_f(st.op(o))
+            self.ctx.check(self.ctx.lib.tn_mps_applyop(self.ctx.h, self._h, s, L.as_dp(m)))
+
+
+class MPOHandle:
+    """Rank-2 GMPS (MPO) on the GPU with its host tensors."""
+
+    rank = 2
+
+    def __init__(self, tensors, ctx=None):
+        self.ctx = ctx or L.context()
+        ts = [L.cplx_f(t) for t in tensors]
+        self.tensors = ts
+        self.N = len(ts)
+        self.dim = ts[0].shape[1]
+        w = [ts[0].shape[0]] + [t.shape[3] for t in ts]
+        self.wdims = w
+        h = C.c_void_p()
+        arr = (C.c_int64 * (self.N + 1))(*w)
+        self.ctx.check(self.ctx.lib.tn_mpo_upload(self.ctx.h, self.N, self.dim, arr, L.ptr_array(ts), C.byref(h)))
+        self._h = h
+
+    def __len__(self):
+        return self.N
+
+    def __getitem__(self, i):
+        return self.tensors[i - 1]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and self.ctx.h:
+            self.ctx.lib.tn_mpo_destroy(h)
+            self._h = None
+
+
+def MPO(st: Sitetypes, H, cutoff=1e-15, ctx=None):
+    """MPO(st, H::OpList) (mpo.jl:323-459), uploaded to the GPU."""
+    return MPOHandle(mpo_tensors(st, H, cutoff), ctx)
+
+
+def randomMPS(dim, length, bonddim, rng=None, draws=None, ctx=None):
+    """randomGMPS (gmps.jl:276-291): normal site tensors (edges 1),
+    movecenter!(N), movecenter!(1), site 1 replaced by a fresh normal
+    [1, d, min(d, bonddim)] tensor, normalize!.  ``draws`` may give the N+1
+    real arrays explicitly; otherwise they come from ``rng`` (numpy
+    Generator), filled in column-major order."""
+    N = length
+    shapes = [((1 if i == 0 else bonddim), dim, (1 if i == N - 1 else bonddim)) for i in range(N)]
+    first = (1, dim, min(dim, bonddim))
+    if draws is None:
+        rng = rng if rng is not None else np.random.default_rng()
+        draws = [_f(rng.standard_normal(int(np.prod(s))), s) for s in shapes]
+        draws.append(_f(rng.standard_normal(int(np.prod(first))), first))
+    psi = GMPS.from_tensors(draws[:N], 0, ctx)
+    psi.movecenter(N)
+    psi.movecenter(1)
+    ts = psi.tensors()
+    ts[0] = draws[N]
+    c = psi.center
+    psi2 = GMPS.from_tensors(ts, c, ctx)
+    psi2.normalize()
+    return psi2
+
+
+def productMPS(st, names, ctx=None):
+    """productMPS(st, names) (mps.jl:68-76); centre unset."""
+    return GMPS.from_tensors([_f(st.state(n), (1, st.dim, 1)) for n in names], 0, ctx)
+
+
+def _terms(st, oplist, d):
+    firsts, lens, mats, coeffs = [], [], [], []
+    for ops, sites, c in zip(oplist.ops, oplist.sites, oplist.coeffs):
+        firsts.append(sites[0])
+        n = sites[-1] - sites[0] + 1
+        lens.append(n)
+        for s in range(sites[0], sites[-1] + 1):
+            m = st.op(ops[sites.index(s)]) if s in sites else np.eye(d, dtype=np.complex128)
+            mats.append(L.cplx_f(m))
+        coeffs.append(complex(c))
+    return firsts, lens, mats, coeffs
+
+
+def inner(st, psi, oplist, phi):
+    """Per-term <psi|term|phi> (mps.jl:87-134), computed on the GPU."""
+    ctx = psi.ctx
+    firsts, lens, mats, coeffs = _terms(st, oplist, psi.dim)
+    n = len(firsts)
+    if n == 0:
+        return np.zeros(0, dtype=np.complex128)
+    f = np.asarray(firsts, dtype=np.int32)
+    ln = np.asarray(lens, dtype=np.int32)
+    ops = np.concatenate([m.ravel(order="F") for m in mats]).astype(np.complex128)
+    co = np.asarray(coeffs, dtype=np.complex128)
+    out = np.zeros(n, dtype=np.complex128)
+    ctx.check(ctx.lib.tn_inner_terms(ctx.h, psi._h, phi._h, n, f.ctypes.data_as(L.i32p),
+                                     ln.ctypes.data_as(L.i32p), L.as_dp(ops), L.as_dp(co), L.as_dp(out)))
+    return out
+
+
+def entropy(psi, site):
+    return psi.entropy(site)
+
+
+def normalize(psi):
+    psi.normalize()
+
+
+def movecenter(psi, idx, **kw):
+    psi.movecenter(idx, **kw)

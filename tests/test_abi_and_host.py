@@ -1,0 +1,145 @@
+"""CPU checks: the C-ABI library loads and exports every declared symbol, and
+the host-side model builders (MPO assembly, Trotter gates) agree with the
+oracle.  No compute call reaches the GPU here."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import exact as X
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "tngpu.h")
+LIB = os.path.join(ROOT, "tensornetworks.jl_gb300", "tngpu", "libtngpu.so")
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int32_t|int64_t|const char\*)\s+(tn_\w+)\s*\(", txt, re.M)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    if not os.path.exists(LIB):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("graft_entry", os.path.join(ROOT, "__graft_entry__.py"))
+        m = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        m.build()
+    return LIB
+
+
+def test_library_exports_every_header_symbol(built):
+    lib = ctypes.CDLL(built)
+    names = header_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", built], capture_output=True, text=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}\b", out), f"{n} not exported as a text symbol"
+
+
+def test_python_binding_covers_header(built):
+    from tngpu import _lib
+    assert sorted(_lib.EXPORTED) == header_functions()
+    lib = _lib.load()
+    assert lib.tn_version() >= 100
+
+
+def test_build_targets_sm103a_only():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("tnbuild", os.path.join(ROOT, "tensornetworks.jl_gb300", "build.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    assert m.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def xxz(N, delta=1.0, field=None, mod=None):
+    H = mod.OpList(N)
+    for i in range(1, N):
+        H.add(["x", "x"], [i, i + 1], 1.0)
+        H.add(["y", "y"], [i, i + 1], 1.0)
+        H.add(["z", "z"], [i, i + 1], delta)
+    if field:
+        for i in range(1, N + 1):
+            H.add("z", i, field(i))
+    return H
+
+
+def test_host_mpo_builder_matches_oracle_operator():
+    import tngpu.models as M
+    N = 7
+    for field in (None, lambda i: 0.2 * (-1) ** i):
+        Hp = xxz(N, 0.5, field, M)
+        Ho = xxz(N, 0.5, field, O)
+        W = M.mpo_tensors(M.spinhalf(), Hp)
+        Wo = O.mpo_from_oplist(O.spinhalf(), Ho)
+        g = O.GMPS(2, 2, W)
+        assert np.allclose(X.mpo_to_dense(g), X.mpo_to_dense(Wo), atol=1e-12)
+        assert [t.shape[3] for t in W] == [t.shape[3] for t in Wo.tensors]
+
+
+def test_host_mpo_long_range_terms():
+    import tngpu.models as M
+    N = 6
+    Hp, Ho = M.OpList(N), O.OpList(N)
+    for H in (Hp, Ho):
+        H.add(["z", "x", "z"], [1, 3, 4], 0.7)
+        H.add(["y", "y"], [2, 5], -0.3)
+        H.add("x", 6, 1.1)
+    W = M.mpo_tensors(M.spinhalf(), Hp)
+    dense = X.oplist_to_dense(O.spinhalf(), Ho)
+    assert np.allclose(X.mpo_to_dense(O.GMPS(2, 2, W)), dense, atol=1e-12)
+
+
+def test_host_trotter_rows_match_oracle():
+    import tngpu.models as M
+    N = 9
+    Hp = xxz(N, 0.5, lambda i: 0.2 * (-1) ** i, M)
+    Ho = xxz(N, 0.5, lambda i: 0.2 * (-1) ** i, O)
+    rp = M.trotter_rows(M.spinhalf(), Hp, 0.05, 2, "real")
+    ro = O.trotterize(O.spinhalf(), Ho, 0.05, 2, "real")
+    assert len(rp) == len(ro) == 3
+    for (sp, gp), (so, go) in zip(rp, ro):
+        assert sp == so
+        for a, b in zip(gp, go):
+            assert a.shape == b.shape and np.allclose(a, b, atol=1e-14)
+
+
+def test_host_opprod_and_qjmc_heff():
+    import tngpu.models as M
+    import tngpu.algorithms as A
+    st = M.spinhalf()
+    assert st.opprod(["s+", "s-"]) == "pu"
+    assert st.opprod(["x", "z"]).startswith("temp")
+    N = 4
+    H = M.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1])
+    Lj = M.OpList(N)
+    for i in range(1, N + 1):
+        Lj.add("s-", i, np.sqrt(0.1))
+    heff, rows = A.qjmc_gates(st, H, Lj, 0.01)
+    Ho, Lo = O.OpList(N), O.OpList(N)
+    for i in range(1, N):
+        Ho.add(["z", "z"], [i, i + 1])
+    for i in range(1, N + 1):
+        Lo.add("s-", i, np.sqrt(0.1))
+    _, ro = O.qjmc_gates(O.spinhalf(), Ho, Lo, 0.01)
+    for (sp, gp), (so, go) in zip(rows, ro):
+        assert sp == so
+        for a, b in zip(gp, go):
+            assert np.allclose(a, b, atol=1e-14)
+
+
+def test_product_path_does_not_import_oracle():
+    pkg = os.path.join(ROOT, "tensornetworks.jl_gb300", "tngpu")
+    for f in os.listdir(pkg):
+        if f.endswith(".py"):
+            assert "oracle" not in open(os.path.join(pkg, f)).read(), f
