@@ -178,6 +178,13 @@ int32_t tn_env_right(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t
 /* Theta'[Dl,o1,o2,Dr] = sum G[o1,i1,o2,i2] A1[Dl,i1,k] A2[k,i2,Dr] (gatelist.jl:137-154). */
 int32_t tn_gate2_apply(tn_ctx* ctx, int64_t chil, int64_t chim, int64_t chir, int32_t d,
                        const double* A1, const double* A2, const double* G, double* out);
+/* C[m x n] = op(A) B with A column-major (m x k, or k x m when conj_a, where
+ * op(A) = A^H), B column-major k x n; precision TN_PREC_FP64 runs the FP64
+ * SIMT GEMM, TN_PREC_MIXED the 3xTF32 tcgen05 GEMM.  No reference
+ * counterpart: the contraction primitive under tensors.jl:13-18 exposed for
+ * tests and callers. */
+int32_t tn_gemm(tn_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int32_t conj_a,
+                const double* B, double* C, int32_t precision);
 /* Truncated split of theta[m x n] (tensors.jl:168-227 keep rule).  direction 0:
  * X isometric, Y = S Vt; direction 1: X = U S, Y co-isometric.  X gets m x k,
  * Y k x n, S the k kept singular values; *k in: capacity, out: kept count. */

@@ -26,6 +26,8 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
                     int max_jumps);
 void mixed_unit_heff2(Ctx* ctx, const cplx* L, const cplx* W12, const cplx* R, int64_t cl,
                       int64_t cr, int d, int64_t wl, int64_t wr, const cplx* x, cplx* y);
+void mixed_gemm(Ctx* ctx, int64_t m, int64_t n, int64_t k, const cplx* A, bool conj_a,
+                const cplx* B, cplx* C);
 }  // namespace tn
 
 using namespace tn;
@@ -92,6 +94,8 @@ int32_t tn_ctx_create(int32_t device, tn_ctx** out) {
         TN_CHECK_SOLVER(cusolverDnCreate(&c.solver));
         TN_CHECK_SOLVER(cusolverDnSetStream(c.solver, c.stream));
         TN_CHECK_CUDA(cudaMalloc(&c.d_info, sizeof(int)));
+        TN_CHECK_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
+        TN_CHECK_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
         TN_CHECK_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
         *out = h;
         return TN_OK;
@@ -114,6 +118,7 @@ int32_t tn_ctx_destroy(tn_ctx* h) {
     if (c.stream) cudaStreamSynchronize(c.stream);
     if (c.solver) cusolverDnDestroy(c.solver);
     if (c.d_info) cudaFree(c.d_info);
+    if (c.d_err) cudaFree(c.d_err);
     if (c.h_pinned) cudaFreeHost(c.h_pinned);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
@@ -667,6 +672,27 @@ int32_t tn_gate2_apply(tn_ctx* h, int64_t cl, int64_t cm, int64_t cr, int32_t d,
     zgemm(ctx, OP_N, OP_N, cl * d, d * cr, cm, one, d1.c(), cl * d, 0, dd2.c(), cm, 0, zero, dT.c(), cl * d, 0);
     small_apply(ctx, dT.c(), dO.c(), dM.c(), d2, d2, cl, cr, cl, cl * d2, cl, cl * d2);
     d2h(ctx, out, dO.p, 16 * nT);
+    ctx->sync();
+    TN_API_END
+}
+
+int32_t tn_gemm(tn_ctx* h, int64_t m, int64_t n, int64_t k, const double* A, int32_t conj_a,
+                const double* B, double* Cout, int32_t precision) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(A && B && Cout, "null argument");
+    TN_REQUIRE(m >= 1 && n >= 1 && k >= 1, "bad dimensions");
+    Ctx* ctx = &h->c;
+    DBuf dA(ctx, 16 * (size_t)m * k), dB(ctx, 16 * (size_t)k * n), dC(ctx, 16 * (size_t)m * n);
+    h2d(ctx, dA.p, A, 16 * (size_t)m * k);
+    h2d(ctx, dB.p, B, 16 * (size_t)k * n);
+    if (precision == TN_PREC_MIXED) {
+        mixed_gemm(ctx, m, n, k, dA.c(), conj_a != 0, dB.c(), dC.c());
+    } else {
+        const cplx one = cmk(1, 0), zero = cmk(0, 0);
+        zgemm(ctx, conj_a ? OP_C : OP_N, OP_N, m, n, k, one, dA.c(), conj_a ? k : m, 0, dB.c(), k, 0,
+              zero, dC.c(), m, 0);
+    }
+    d2h(ctx, Cout, dC.p, 16 * (size_t)m * n);
     ctx->sync();
     TN_API_END
 }

@@ -82,6 +82,7 @@ struct Ctx {
     Scratch s_gram, s_eigval, s_work, s_x, s_y, s_t1, s_t2, s_dot, s_coef, s_mixa, s_mixb, s_mixc,
         s_mixd, s_mixe, s_mixf;
     int* d_info = nullptr;
+    int* d_err = nullptr;  // set by device code when a bounded wait runs out
     double* h_pinned = nullptr;  // small pinned staging area
     size_t h_pinned_n = 0;
     void sync() { TN_CHECK_CUDA(cudaStreamSynchronize(stream)); }

@@ -325,6 +325,7 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
             }
             LanczosOut lo = lanczos_lowest(ctx, n, theta.c(), mv, o.krylovdim, o.kryloviter, 1e-14, vec);
             matvecs += lo.numops;
+            if (o.precision == TN_PREC_MIXED) tc_check_error(ctx);
             cost = cmk(lo.eig, 0.0);
             SplitResult sr = replacesites2(psi, vec.c(), site1, direction, true, tr);
             last_disc = sr.discarded;

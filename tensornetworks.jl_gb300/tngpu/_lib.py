@@ -78,6 +78,7 @@ _SIGS = {
     "tn_env_right": (i32, [P, i64, i64, i32, i64, i64, dp, dp, dp, dp, i32]),
     "tn_gate2_apply": (i32, [P, i64, i64, i64, i32, dp, dp, dp, dp]),
     "tn_truncate": (i32, [P, i64, i64, dp, C.POINTER(TruncOpts), i32, dp, dp, dp, i64p]),
+    "tn_gemm": (i32, [P, i64, i64, i64, dp, i32, dp, dp, i32]),
 }
 
 EXPORTED = tuple(_SIGS)

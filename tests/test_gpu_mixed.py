@@ -1,0 +1,94 @@
+"""Mixed-precision path: the 3xTF32 tcgen05 GEMM and the H_eff product built
+on it, compared with FP64 references.  Tolerance: 3xTF32 products with FP32
+accumulation reach ~1e-6 relative; the tests allow 2e-5 relative in the
+Frobenius norm."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+
+@pytest.fixture(scope="module")
+def tn():
+    import tngpu
+    return tngpu
+
+
+def crand(rng, *shape):
+    return np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+
+def dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("m,n,k,conj", [(128, 128, 32, 0), (1, 1, 1, 0), (200, 77, 45, 0),
+                                        (300, 260, 1030, 1), (64, 513, 257, 1), (1024, 640, 2048, 0)])
+def test_tc_gemm(tn, m, n, k, conj):
+    ctx = tn.context()
+    rng = np.random.default_rng(m + n + k)
+    A = crand(rng, k, m) if conj else crand(rng, m, k)
+    B = crand(rng, k, n)
+    Cg = np.zeros((m, n), dtype=np.complex128, order="F")
+    ctx.check(ctx.lib.tn_gemm(ctx.h, m, n, k, dp(A), conj, dp(B), dp(Cg), 1))
+    ref = (A.conj().T if conj else A) @ B
+    assert rel(Cg, ref) < TOL
+    # the FP64 path of the same entry point is exact to rounding
+    C64 = np.zeros_like(Cg)
+    ctx.check(ctx.lib.tn_gemm(ctx.h, m, n, k, dp(A), conj, dp(B), dp(C64), 0))
+    assert rel(C64, ref) < 1e-13
+
+
+@pytest.mark.parametrize("cl,cr,w", [(1, 4, 5), (37, 19, 5), (128, 128, 5), (300, 200, 3), (512, 512, 5)])
+def test_heff2_mixed(tn, cl, cr, w):
+    ctx = tn.context()
+    rng = np.random.default_rng(cl * 7 + cr)
+    d = 2
+    wl = 1 if cl == 1 else w
+    L, W1, W2 = crand(rng, cl, wl, cl), crand(rng, wl, d, d, w), crand(rng, w, d, d, w)
+    R, th = crand(rng, cr, w, cr), crand(rng, cl, d, d, cr)
+    out = np.zeros((cl, d, d, cr), dtype=np.complex128, order="F")
+    ctx.check(ctx.lib.tn_heff2_apply(ctx.h, cl, cr, d, wl, w, w, dp(L), dp(W1), dp(W2), dp(R),
+                                     dp(th), dp(out), 1))
+    ref = O.core.heff2(L, W1, W2, R, th)
+    assert rel(out, ref) < TOL
+
+
+def _xxz(tn, N):
+    H = tn.OpList(N)
+    for i in range(1, N):
+        for o in "xyz":
+            H.add([o, o], [i, i + 1], 1.0)
+    return H
+
+
+def test_dmrg_mixed_matches_fp64(tn):
+    """Mixed-precision DMRG (3xTF32 matvecs, FP64 Lanczos/truncation) against
+    the plain FP64 run from the same state: |dE/E| on the FP64-recomputed
+    energy and identical kept bond dimensions."""
+    N, D = 24, 8
+    rng = np.random.default_rng(3)
+    shapes = [((1 if i == 0 else D), 2, (1 if i == N - 1 else D)) for i in range(N)]
+    draws = [O.fr(rng.standard_normal(int(np.prod(s))), s) for s in shapes]
+    draws.append(O.fr(rng.standard_normal(4), (1, 2, 2)))
+    po = O.random_mps(2, N, D, draws)
+    W = tn.MPO(tn.spinhalf(), _xxz(tn, N))
+    kw = dict(maxdim=128, cutoff=1e-12, minsweeps=8, maxsweeps=8, numconverges=np.inf, verbose=False)
+    p64 = tn.GMPS.from_tensors(po.tensors, po.center)
+    _, E64 = tn.dmrg(p64, W, **kw)
+    pmx = tn.GMPS.from_tensors(po.tensors, po.center)
+    st = {}
+    _, Emx = tn.dmrg(pmx, W, precision="mixed", stats=st, **kw)
+    assert abs(st["energy_fp64"] - E64) <= 1e-8 * abs(E64), (st["energy_fp64"], E64, Emx)
+    assert abs(Emx - E64) <= 1e-5 * abs(E64)
