@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Two-site DMRG sweeps/s at chi=1024 on the Heisenberg XXZ chain (N=100,
+J=Delta=1, open boundaries, MPO bond dimension 5), mixed precision:
+3xTF32 tcgen05 tensor-core H_eff products, FP64 Lanczos, environments and
+truncation.
+
+Workload: seeded random MPS of bond dimension 16 (numpy PCG64 seed 2),
+ramped with maxdim 64 (2 sweeps) and 256 (2 sweeps), then W warm-up and K
+timed sweeps at maxdim=1024, cutoff 1e-12, krylovdim=3, kryloviter=2.  A
+sweep is one directional pass (dmrg.jl:66).  Inputs (MPS 2.7 GB, environment
+blocks up to 80 MB each) are far larger than L2; no flush needed.
+
+Reported beside it: an FP64 bond-update sample of the same state (plain FP64
+path), an end-to-end run through the C ABI from pinned host buffers, the
+kernel roofline from the library's CUDA-event profiler, and a CPU baseline
+(the numpy FP64 restatement of the reference, one bond update at chi=1024).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tensornetworks.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "DMRG sweeps/s at chi=1024 (mixed vs FP64, |dE|<1e-9); QJMC trajectory-steps/s"
+UNIT = "sweeps/s"
+N_SITES, CHI, D0, SEED = 100, 1024, 16, 2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=N_SITES)
+    p.add_argument("--chi", type=int, default=CHI)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def config(args):
+    return {"workload": f"XXZ chain N={args.n} J=Delta=1 OBC, two-site DMRG at maxdim={args.chi} "
+                        f"after a 64/256 ramp, cutoff 1e-12, krylovdim 3, kryloviter 2",
+            "model": "Heisenberg XXZ MPO (w=5)", "n_sites": args.n, "chi": args.chi,
+            "initial_state": f"random MPS D={D0}, numpy PCG64 seed {SEED}",
+            "l2": "working set > L2 (MPS 2.7 GB, environments up to 80 MB each); no flush",
+            "parallelism": "replicas only (bond-sequential sweeps)"}
+
+
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def xxz(mod, N):
+    H = mod.OpList(N)
+    for i in range(1, N):
+        for o in "xyz":
+            H.add([o, o], [i, i + 1], 1.0)
+    return H
+
+
+def draws(N, D, seed):
+    rng = np.random.default_rng(seed)
+    shapes = [((1 if i == 0 else D), 2, (1 if i == N - 1 else D)) for i in range(N)]
+    out = [np.reshape(rng.standard_normal(int(np.prod(s))), s, order="F") for s in shapes]
+    out.append(np.reshape(rng.standard_normal(2 * min(2, D)), (1, 2, min(2, D)), order="F"))
+    return out
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi samples (200 ms) while a region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={device}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 9]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        util = [float(r[4]) for r in rows if r[4].strip().replace(".", "").isdigit()]
+        loaded = [s for s, u in zip(sm, util) if u >= 20] or sm
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[6:10]) if "Active" in v and "Not" not in v})
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_bond_sample(chi, w=5, d=2, seed=0):
+    """One two-site bond update of the FP64 CPU restatement at chi: Lanczos
+    (krylovdim 3, 2 cycles: 5 matvecs), truncated SVD to chi, one environment
+    update.  Environment blocks are Hermitian per channel, synthetic."""
+    import oracle as O
+    rng = np.random.default_rng(seed)
+
+    def herm_env(c):
+        X = rng.standard_normal((c, w, c)) + 1j * rng.standard_normal((c, w, c))
+        return X + np.conj(np.transpose(X, (2, 1, 0)))
+
+    L, R = herm_env(chi), herm_env(chi)
+    st = O.spinhalf()
+    W = O.mpo_from_oplist(st, xxz(O, 8))[4]  # a bulk tensor, w = 5 on both sides
+    theta = rng.standard_normal((chi, d, d, chi)) + 1j * rng.standard_normal((chi, d, d, chi))
+    t0 = time.perf_counter()
+    _, vec = O.lanczos_lowest(lambda x: O.core.heff2(L, W, W, R, x), theta, 3, 2)
+    M = O.fr(vec, (chi * d, d * chi))
+    U, S, Vt = O.trunc_svd(M, 1e-12, chi, 1)
+    A = O.fr(U, (chi, d, U.shape[1]))
+    O.core.env_left(L, A, W, A)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args):
+    """The reference's CPU path on the host cores: Julia is not installed, so
+    this times the numpy FP64 restatement (the oracle) with all host BLAS
+    threads, one bond update at chi per step, reported as sweeps/s."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_bond_sample(min(args.chi, 256))
+    ts = [cpu_bond_sample(args.chi, seed=i) for i in range(args.steps)]
+    t = float(np.mean(ts))
+    value = 1.0 / (t * (args.n - 1))
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(args),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"one bond update at chi={args.chi} per step (5 Lanczos "
+                                       f"matvecs, SVD, env update), extrapolated x{args.n - 1} "
+                                       "bonds; Julia absent, numpy FP64 restatement"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def ours(args):
+    import ctypes as C
+
+    import tngpu as tn
+    from tngpu import _lib as L
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    ctx = tn.Context(local)
+    W_mpo = tn.MPO(tn.spinhalf(), xxz(tn, args.n), ctx=ctx)
+    psi = tn.randomMPS(2, args.n, D0, draws=draws(args.n, D0, SEED), ctx=ctx)
+    ramp = {}
+    for md in (64, 256):
+        t0 = time.perf_counter()
+        tn.dmrg(psi, W_mpo, maxdim=md, cutoff=1e-12, minsweeps=2, maxsweeps=2, numconverges=np.inf,
+                verbose=False, precision="mixed")
+        ramp[md] = time.perf_counter() - t0
+
+    Wu, K = args.warmup, args.steps
+    if dist:
+        dist.barrier()
+    clk = Clocks(local)
+    st = {}
+    t0 = time.perf_counter()
+    # an even number of directional sweeps leaves the centre at site 1, so the
+    # FP64 sample and the end-to-end run start without re-canonicalising
+    total = Wu + K + (Wu + K) % 2
+    _, E = tn.dmrg(psi, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=total, maxsweeps=total,
+                   numconverges=np.inf, verbose=False, precision="mixed", stats=st,
+                   profile_from_sweep=Wu)
+    wall_main = time.perf_counter() - t0
+    clocks = clk.stop()
+    log(f"main: {wall_main:.1f} s, sweeps {['%.2f' % s for s in st['sweep_seconds']]}, "
+        f"maxdim {st['sweep_maxdim']}, E={E:.12f}, E64={st['energy_fp64']:.12f}, ramp {ramp}")
+    timed = st["sweep_seconds"][Wu:Wu + K]
+    t_timed = float(sum(timed))
+    if dist:
+        import torch
+        tt = torch.tensor([t_timed], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_timed = float(tt.item())
+    value = world * K / t_timed
+
+    # kernel profile of the timed sweeps
+    n = L.TN_PROF if hasattr(L, "TN_PROF") else 8
+    la, ms, fl, by = (C.c_int64 * n)(), (C.c_double * n)(), (C.c_double * n)(), (C.c_double * n)()
+    ctx.check(ctx.lib.tn_profile_read(ctx.h, la, ms, fl, by))
+    prof = [{"kernel": L.PROF_CLASSES[i], "launches": int(la[i]), "ms": ms[i], "flops": fl[i],
+             "bytes": by[i]} for i in range(n)]
+    gpu_launches = int(la[7])
+
+    pk, pk_src = peaks()
+    tf32_peak = 0.5 * pk["bf16_tflops"]
+    tc = prof[0]
+    tc_achieved = 3.0 * tc["flops"] / (tc["ms"] * 1e-3) / 1e12 if tc["ms"] > 0 else 0.0
+    roof_tc = {"kernel": tc["kernel"], "bound": "tensor", "achieved": tc_achieved, "peak": tf32_peak,
+               "unit": "TFLOP/s", "frac": tc_achieved / tf32_peak, "traffic": None,
+               "launches": tc["launches"], "avg_launch_ms": tc["ms"] / max(tc["launches"], 1),
+               "note": "achieved counts the three TF32 passes the tensor pipe executes "
+                       "(3 x 8 flops per complex multiply-add); peak = 0.5 x "
+                       f"{pk_src} bf16 dense ({pk['bf16_tflops']} TF/s): TF32 runs at half the "
+                       "BF16 rate"}
+    own = [p for i, p in enumerate(prof) if i not in (2, 7)]
+    dom = max(own, key=lambda p: p["ms"])
+    roof = roof_tc
+    if dom is not tc and dom["kernel"].startswith("zgemm"):
+        # FP64 SIMT GEMM: the FP64 peak is not in the measured-peaks file;
+        # cuBLAS ZGEMM 4096^3 is timed here as the denominator
+        z_peak = cublas_zgemm_tflops(local)
+        ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+        roof = {"kernel": dom["kernel"], "bound": "fp64-pipe", "achieved": ach, "peak": z_peak,
+                "unit": "TFLOP/s", "frac": ach / z_peak if z_peak else None, "traffic": None,
+                "launches": dom["launches"], "avg_launch_ms": dom["ms"] / max(dom["launches"], 1),
+                "note": "peak = cuBLAS ZGEMM 4096^3 measured in this run (the measured-peaks file "
+                        "has no FP64 figure)"}
+
+    # FP64 comparison: bond-update sample of the same state, plain FP64 path
+    log("profile: " + json.dumps(prof))
+    fp64 = fp64_sample(tn, psi, W_mpo, args, st)
+    log("fp64 sample: " + json.dumps(fp64))
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": Wu, "ms_per_step": 1e3 * t_timed / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed(tf32x3 tensor-core, f64)",
+            "data": "synthetic", "config": config(args), "clocks": clocks,
+            "gpu_launches": gpu_launches, "roofline": roof, "roofline_tensor_core": roof_tc,
+            "energy": {"lanczos": E, "fp64_rayleigh": st["energy_fp64"],
+                       "rel_diff": abs(E - st["energy_fp64"]) / abs(st["energy_fp64"])},
+            "sweeps": {"seconds": st["sweep_seconds"], "maxdim": st["sweep_maxdim"],
+                       "energies": st["sweep_energies"], "ramp_seconds": ramp,
+                       "main_wall_s": wall_main},
+            "fp64": fp64, "kernel_profile": prof}
+    if fp64.get("sweeps_per_s_est"):
+        line["mixed_vs_fp64"] = value / world / fp64["sweeps_per_s_est"]
+    if not args.no_e2e:
+        line["e2e"] = e2e_run(tn, ctx, psi, W_mpo, args, world)
+        log("e2e: " + json.dumps(line["e2e"]))
+    if rank == 0 and not args.no_cpu:
+        t = cpu_bond_sample(args.chi)
+        line["cpu_baseline"] = {"value": 1.0 / (t * (args.n - 1)), "unit": UNIT,
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"one bond update at chi={args.chi} ({t:.1f} s: 5 Lanczos "
+                                          f"matvecs, SVD, env update), x{args.n - 1} bonds; numpy "
+                                          "FP64 restatement (Julia absent)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cublas_zgemm_tflops(device):
+    try:
+        import torch
+        a = torch.randn(4096, 4096, dtype=torch.complex128, device=f"cuda:{device}")
+        b = torch.randn_like(a)
+        a @ b
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(2):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        return 2 * 8 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
+def fp64_sample(tn, psi, W_mpo, args, st_mixed, nbonds=14):
+    """Plain FP64 DMRG bond updates from the chi=1024 state (the first
+    `nbonds` of a right sweep, which reach the bulk chi); the FP64 sweep time
+    is estimated from the bulk per-bond time scaled by each bond's chi^3."""
+    p = psi.copy()
+    st = {}
+    tn.dmrg(p, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=1, maxsweeps=1, numconverges=np.inf,
+            verbose=False, precision="fp64", stats=st, max_bond_updates=nbonds)
+    secs, chis = np.asarray(st["bond_seconds"]), np.asarray(st["bond_chi"])
+    bulk = secs[chis == chis.max()]
+    per_bulk = float(bulk[1:].mean() if bulk.size > 1 else bulk.mean())
+    dims = p.bonddims()
+    chi_b = [max(dims[i], dims[i + 2]) for i in range(len(dims) - 2)]
+    est = sum(per_bulk * (c / chis.max()) ** 3 for c in chi_b)
+    return {"bond_seconds": secs.tolist(), "bond_chi": chis.tolist(), "bulk_bond_s": per_bulk,
+            "sweep_s_est": est, "sweeps_per_s_est": 1.0 / est,
+            "method": f"{nbonds} FP64 bond updates; sweep = sum over bonds of the bulk time x (chi/chi_max)^3"}
+
+
+def e2e_run(tn, ctx, psi, W_mpo, args, world):
+    """K sweeps through the C ABI from pinned host buffers: upload the MPS,
+    tn_dmrg (mixed, K sweeps), download the MPS, all inside the timed region."""
+    import ctypes as C
+
+    import torch
+    from tngpu import _lib as L
+    K = args.steps
+    ts = psi.tensors()
+    pinned = [torch.empty(t.size * 2, dtype=torch.float64, pin_memory=True) for t in ts]
+    views = []
+    for t, pbuf in zip(ts, pinned):
+        v = pbuf.numpy().view(np.complex128).reshape(t.shape, order="F")
+        v[...] = t
+        views.append(v)
+    dims = (C.c_int64 * (len(ts) + 1))(*psi.bonddims())
+    nbytes = sum(t.nbytes for t in ts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h = C.c_void_p()
+    ctx.check(ctx.lib.tn_mps_upload(ctx.h, len(ts), 2, dims, L.ptr_array(views), psi.center, C.byref(h)))
+    g = tn.GMPS(h, len(ts), 2, ctx)
+    tn.dmrg(g, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=K, maxsweeps=K, numconverges=np.inf,
+            verbose=False, precision="mixed")
+    out = g.bonddims()
+    outs = []
+    for i in range(len(ts)):
+        nb = out[i] * 2 * out[i + 1] * 2
+        outs.append(torch.empty(nb, dtype=torch.float64, pin_memory=True))
+    ctx.check(ctx.lib.tn_mps_download(ctx.h, g._h, (L.dp * len(outs))(*[
+        C.cast(o.data_ptr(), L.dp) for o in outs])))
+    t = time.perf_counter() - t0
+    dbytes = sum(o.numel() * 8 for o in outs)
+    return {"value": world * K / t, "unit": UNIT, "h2d_bytes_per_step": nbytes // K,
+            "d2h_bytes_per_step": dbytes // K,
+            "note": "upload + tn_dmrg(K sweeps; re-canonicalises and rebuilds environments) + "
+                    "download, pinned host buffers"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

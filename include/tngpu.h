@@ -67,6 +67,8 @@ typedef struct tn_dmrg_opts {
     int32_t verbose;       /* print the reference's per-sweep line        */
     int32_t max_bond_updates; /* 0 = run the sweeps; n > 0 = stop after n bond
                                  optimisations (a bounded timing sample)  */
+    int32_t profile_from_sweep; /* >= 0: enable the kernel profiler (see
+                                   tn_profile_read) from this sweep index on */
 } tn_dmrg_opts;
 
 typedef struct tn_dmrg_stats {
@@ -84,7 +86,22 @@ typedef struct tn_dmrg_stats {
     double* sweep_energies;
     int32_t* sweep_maxdim;
     int32_t bond_updates;  /* bond optimisations performed */
+    int32_t bond_cap;      /* optional per-bond records, capacity bond_cap */
+    double* bond_seconds;  /* host wall seconds of each bond optimisation */
+    int32_t* bond_chi;     /* max(chi_l, chi_r) of each optimised bond */
 } tn_dmrg_stats;
+
+/* ---- kernel profiler ---------------------------------------------------------
+ * CUDA events on the context's stream around each launch of a kernel class;
+ * algorithmic flops and bytes are accumulated per class.  Classes:
+ * 0 tensor-core GEMM (tcgen05), 1 FP64 GEMM, 2 Hermitian eigensolver,
+ * 3 FP64 operator legs, 4 mixed operator leg, 5 operand conversion,
+ * 6 Lanczos vector ops; class 7 holds only a launch count: every kernel this
+ * library launched while the profiler was on. */
+#define TN_PROF_CLASSES 8
+int32_t tn_profile_enable(tn_ctx* ctx, int32_t on);
+int32_t tn_profile_reset(tn_ctx* ctx);
+int32_t tn_profile_read(tn_ctx* ctx, int64_t* launches, double* ms, double* flops, double* bytes);
 
 /* ---- context -------------------------------------------------------------- */
 int32_t tn_ctx_create(int32_t device, tn_ctx** out);
@@ -162,6 +179,20 @@ int32_t tn_qjmc_run(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nju
                     const tn_trunc_opts* trunc, int32_t save_every, int32_t nobs,
                     const int32_t* obs_sites, const double* obs_ops, double* obs_out,
                     int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used);
+
+/* ntraj independent trajectories of the run above from the same initial MPS,
+ * advanced concurrently by nworkers host threads, each with its own CUDA
+ * stream; trajectory t consumes draws[t*ndraws_per_traj ...].  obs_avg gets
+ * the trajectory-averaged observables (rows = t=0 and every save_every
+ * steps, nobs columns, re/im); njumps_per_traj (optional) the jump counts.
+ * The reference runs one trajectory per qjmc_simulation call (qjmc.jl:28);
+ * ensembles are this loop. */
+int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, int32_t njump,
+                      const int32_t* jump_sites, const double* jump_ops, const double* jump_coeffs,
+                      int32_t nsteps, double dt, int32_t ntraj, const double* draws,
+                      int64_t ndraws_per_traj, const tn_trunc_opts* trunc, int32_t save_every,
+                      int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
+                      double* obs_avg, int32_t* njumps_per_traj, int32_t nworkers);
 
 /* ---- unit-level kernels on host buffers (for parity tests) --------------- */
 /* out[a,s1',s2',c'] = sum L[a,w,b] W1[w,s1',s1,w'] W2[w',s2',s2,w''] th[b,s1,s2,c] R[c',w'',c]

@@ -514,16 +514,24 @@ def env_left(L, A, W, B):
     """L'[a',w',b'] = sum L[a,w,b] conj(A[a,s',a']) W[w,s',s,w'] B[b,s,b']
     (projmps.jl:50-66).  W None gives the rank-1 overlap block L'[a',b']."""
     if W is None:
-        return np.einsum("ab,asc,bsd->cd", L, np.conj(A), B, optimize=True)
-    return np.einsum("awb,atc,wtsv,bsd->cvd", L, np.conj(A), W, B, optimize=True)
+        t = np.tensordot(L, np.conj(A), axes=([0], [0]))            # b, s, a'
+        return np.tensordot(t, B, axes=([0, 1], [0, 1]))            # a', b'
+    t = np.tensordot(L, np.conj(A), axes=([0], [0]))                # w, b, s', a'
+    t = np.tensordot(t, W, axes=([0, 2], [0, 1]))                   # b, a', s, w'
+    t = np.tensordot(t, B, axes=([0, 2], [0, 1]))                   # a', w', b'
+    return t
 
 
 def env_right(R, A, W, B):
     """R[a,w,b] = sum B[b,s,b'] R[a',w',b'] W[w,s',s,w'] conj(A[a,s',a'])
     (projmps.jl:74-95)."""
     if W is None:
-        return np.einsum("cd,asc,bsd->ab", R, np.conj(A), B, optimize=True)
-    return np.einsum("cvd,atc,wtsv,bsd->awb", R, np.conj(A), W, B, optimize=True)
+        t = np.tensordot(B, R, axes=([2], [1]))                     # b, s, a'
+        return np.tensordot(np.conj(A), t, axes=([1, 2], [1, 2]))   # a, b
+    t = np.tensordot(B, R, axes=([2], [2]))                         # b, s, a', w'
+    t = np.tensordot(W, t, axes=([2, 3], [1, 3]))                   # w, s', b, a'
+    t = np.tensordot(np.conj(A), t, axes=([1, 2], [1, 3]))          # a, w, b
+    return t
 
 
 def heff2(L, W1, W2, R, theta):

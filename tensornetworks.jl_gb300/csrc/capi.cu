@@ -28,6 +28,11 @@ void mixed_unit_heff2(Ctx* ctx, const cplx* L, const cplx* W12, const cplx* R, i
                       int64_t cr, int d, int64_t wl, int64_t wr, const cplx* x, cplx* y);
 void mixed_gemm(Ctx* ctx, int64_t m, int64_t n, int64_t k, const cplx* A, bool conj_a,
                 const cplx* B, cplx* C);
+void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsites,
+                const double* jops, const double* jcoeffs, int nsteps, double dt, int ntraj,
+                const double* draws, int64_t ndraws_per_traj, const Trunc& t, int save_every,
+                int nobs, const int* obs_sites, const double* obs_ops, double* obs_avg,
+                int* njumps_per_traj, int nworkers);
 }  // namespace tn
 
 using namespace tn;
@@ -83,20 +88,13 @@ int32_t tn_ctx_create(int32_t device, tn_ctx** out) {
         int ndev = 0;
         TN_CHECK_CUDA(cudaGetDeviceCount(&ndev));
         TN_REQUIRE(device >= 0 && device < ndev, "device index out of range");
-        TN_CHECK_CUDA(cudaSetDevice(device));
         tn_ctx* h = new tn_ctx();
-        Ctx& c = h->c;
-        c.device = device;
-        TN_CHECK_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-        TN_CHECK_CUDA(cudaDeviceGetDefaultMemPool(&c.pool, device));
-        uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
-        TN_CHECK_CUDA(cudaMemPoolSetAttribute(c.pool, cudaMemPoolAttrReleaseThreshold, &thr));
-        TN_CHECK_SOLVER(cusolverDnCreate(&c.solver));
-        TN_CHECK_SOLVER(cusolverDnSetStream(c.solver, c.stream));
-        TN_CHECK_CUDA(cudaMalloc(&c.d_info, sizeof(int)));
-        TN_CHECK_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
-        TN_CHECK_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
-        TN_CHECK_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
+        try {
+            ctx_init(h->c, device);
+        } catch (...) {
+            delete h;
+            throw;
+        }
         *out = h;
         return TN_OK;
     } catch (const tn::Error& e) {
@@ -107,20 +105,7 @@ int32_t tn_ctx_create(int32_t device, tn_ctx** out) {
 
 int32_t tn_ctx_destroy(tn_ctx* h) {
     if (!h) return TN_OK;
-    Ctx& c = h->c;
-    cudaSetDevice(c.device);
-    if (c.stream) cudaStreamSynchronize(c.stream);
-    // scratch buffers release through the stream before it goes away
-    c.s_gram.buf.reset(); c.s_eigval.buf.reset(); c.s_work.buf.reset(); c.s_x.buf.reset();
-    c.s_y.buf.reset(); c.s_t1.buf.reset(); c.s_t2.buf.reset(); c.s_dot.buf.reset();
-    c.s_coef.buf.reset(); c.s_mixa.buf.reset(); c.s_mixb.buf.reset(); c.s_mixc.buf.reset();
-    c.s_mixd.buf.reset(); c.s_mixe.buf.reset(); c.s_mixf.buf.reset();
-    if (c.stream) cudaStreamSynchronize(c.stream);
-    if (c.solver) cusolverDnDestroy(c.solver);
-    if (c.d_info) cudaFree(c.d_info);
-    if (c.d_err) cudaFree(c.d_err);
-    if (c.h_pinned) cudaFreeHost(c.h_pinned);
-    if (c.stream) cudaStreamDestroy(c.stream);
+    ctx_release(h->c);
     delete h;
     return TN_OK;
 }
@@ -128,6 +113,34 @@ int32_t tn_ctx_destroy(tn_ctx* h) {
 const char* tn_last_error(tn_ctx* h) { return h ? h->c.err.c_str() : g_noctx_err.c_str(); }
 
 int64_t tn_kernel_launches(tn_ctx* h) { return h ? h->c.launches : 0; }
+
+int32_t tn_profile_enable(tn_ctx* h, int32_t on) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h, "null argument");
+    h->c.prof_on = on != 0;
+    TN_API_END
+}
+
+int32_t tn_profile_reset(tn_ctx* h) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h, "null argument");
+    h->c.prof_flush();
+    for (auto& c : h->c.prof) c = Ctx::ProfClass{};
+    TN_API_END
+}
+
+int32_t tn_profile_read(tn_ctx* h, int64_t* launches, double* ms, double* flops, double* bytes) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h && launches && ms && flops && bytes, "null argument");
+    h->c.prof_flush();
+    for (int i = 0; i < TN_PROF_CLASSES; ++i) {
+        launches[i] = h->c.prof[i].launches;
+        ms[i] = h->c.prof[i].ms;
+        flops[i] = h->c.prof[i].flops;
+        bytes[i] = h->c.prof[i].bytes;
+    }
+    TN_API_END
+}
 
 // ---- MPS ----------------------------------------------------------------------
 int32_t tn_mps_upload(tn_ctx* h, int32_t N, int32_t d, const int64_t* bonddims,
@@ -526,6 +539,22 @@ int32_t tn_qjmc_run(tn_ctx* h, tn_mps* psi, const tn_gates* g, int32_t njump,
     }
     *njumps = (int32_t)r.jumps.size();
     if (ndraws_used) *ndraws_used = r.used;
+    TN_API_END
+}
+
+int32_t tn_qjmc_batch(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32_t njump,
+                      const int32_t* jump_sites, const double* jump_ops, const double* jump_coeffs,
+                      int32_t nsteps, double dt, int32_t ntraj, const double* draws,
+                      int64_t ndraws_per_traj, const tn_trunc_opts* t, int32_t save_every,
+                      int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
+                      double* obs_avg, int32_t* njumps_per_traj, int32_t nworkers) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(psi0 && g && draws && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
+    TN_REQUIRE(nsteps >= 0 && njump >= 1 && nobs >= 0, "bad counts");
+    TN_REQUIRE(nobs == 0 || (obs_sites && obs_ops), "null observables");
+    qjmc_batch(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
+               ndraws_per_traj, to_trunc(t), save_every, nobs, obs_sites, obs_ops, obs_avg,
+               njumps_per_traj, nworkers);
     TN_API_END
 }
 

@@ -85,10 +85,56 @@ struct Ctx {
     int* d_err = nullptr;  // set by device code when a bounded wait runs out
     double* h_pinned = nullptr;  // small pinned staging area
     size_t h_pinned_n = 0;
+    // kernel profiler: CUDA events around launches, per class
+    struct ProfClass {
+        int64_t launches = 0;
+        double ms = 0, flops = 0, bytes = 0;
+    };
+    struct ProfRec {
+        int cls;
+        cudaEvent_t a, b;
+        double flops, bytes;
+    };
+    bool prof_on = false;
+    ProfClass prof[TN_PROF_CLASSES];
+    std::vector<ProfRec> prof_pending;
+    std::vector<cudaEvent_t> ev_pool;
+    cudaEvent_t ev_get();
+    void prof_flush();  // resolves pending event pairs (synchronises)
     void sync() { TN_CHECK_CUDA(cudaStreamSynchronize(stream)); }
-    void count() { ++launches; }
+    void count() {
+        ++launches;
+        if (prof_on) ++prof[TN_PROF_CLASSES - 1].launches;  // class 7 counts every launch
+    }
     double* pinned(size_t n);
 };
+
+// Records a CUDA event pair around the launches in its scope when the
+// context's profiler is on.
+struct ProfScope {
+    Ctx* ctx;
+    int cls;
+    double flops, bytes;
+    cudaEvent_t a = nullptr;
+    ProfScope(Ctx* c, int k, double f, double b) : ctx(c), cls(k), flops(f), bytes(b) {
+        if (ctx->prof_on) {
+            a = ctx->ev_get();
+            cudaEventRecord(a, ctx->stream);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = ctx->ev_get();
+            cudaEventRecord(b, ctx->stream);
+            ctx->prof_pending.push_back({cls, a, b, flops, bytes});
+            if (ctx->prof_pending.size() > 4096) ctx->prof_flush();
+        }
+    }
+};
+
+// stream, solver handle, pool settings and device flags of a context
+void ctx_init(Ctx& c, int device);
+void ctx_release(Ctx& c);
 
 // ---- small complex helpers ----------------------------------------------
 __host__ __device__ inline cplx cmk(double r, double i) { return make_double2(r, i); }

@@ -296,12 +296,18 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
     } evg{ev0, ev1};
     while (!converged) {
+        if (o.profile_from_sweep >= 0 && sweeps == o.profile_from_sweep) {
+            ctx->prof_flush();
+            for (auto& c : ctx->prof) c = Ctx::ProfClass{};
+            ctx->prof_on = true;
+        }
         TN_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
         for (int j = 1; j <= N - 1; ++j) {
             if (o.max_bond_updates > 0 && bond_updates >= o.max_bond_updates) {
                 sample_done = true;
                 break;
             }
+            const auto tb0 = std::chrono::steady_clock::now();
             const int site = direction ? N + 1 - j : j;
             const int site1 = direction ? site - 1 : site;
             env.movecenter(site);
@@ -329,6 +335,12 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
             cost = cmk(lo.eig, 0.0);
             SplitResult sr = replacesites2(psi, vec.c(), site1, direction, true, tr);
             last_disc = sr.discarded;
+            if (stats && bond_updates < stats->bond_cap) {
+                if (stats->bond_seconds)
+                    stats->bond_seconds[bond_updates] =
+                        std::chrono::duration<double>(std::chrono::steady_clock::now() - tb0).count();
+                if (stats->bond_chi) stats->bond_chi[bond_updates] = (int32_t)std::max(cl, cr);
+            }
             ++bond_updates;
         }
         if (sample_done) break;
@@ -362,6 +374,10 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         lastcost = cost;
         lastD = D;
         if (o.verbose) printf("Sweep=%d, energy=%.12f, maxbonddim=%d \n", sweeps, cost.x, D);
+    }
+    if (o.profile_from_sweep >= 0 && ctx->prof_on) {
+        ctx->prof_flush();
+        ctx->prof_on = false;
     }
     double e64 = cost.x;
     if (o.precision == TN_PREC_MIXED && !sample_done) {

@@ -446,6 +446,8 @@ void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha
     if (k <= 0) {  // C = beta * C
         alpha = cmk(0, 0);
     }
+    ProfScope ps(ctx, 1, 8.0 * m * n * (double)std::max<int64_t>(k, 0) * batch,
+                 16.0 * (double)(m * k + k * n + m * n) * batch);
     switch (opa) {
         case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
         case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
@@ -462,6 +464,7 @@ void small_apply(Ctx* ctx, const cplx* in, cplx* out, const cplx* M, int nI, int
     if (na <= 0 || nc <= 0) return;
     TN_REQUIRE(nI * nJ <= 4096, "small_apply: operator too large");
     const size_t smem = sizeof(cplx) * nI * nJ;
+    ProfScope ps(ctx, 3, 8.0 * na * nc * nI * nJ, 16.0 * na * nc * (nI + nJ));
     small_apply_kernel<<<grid_for(ctx, na * nc), 256, smem, ctx->stream>>>(
         in, out, M, nI, nJ, na, nc, lda_i, ldc_i, lda_o, ldc_o, accumulate ? 1 : 0);
     ctx->count();
@@ -469,6 +472,7 @@ void small_apply(Ctx* ctx, const cplx* in, cplx* out, const cplx* M, int nI, int
 }
 
 void multi_dot(Ctx* ctx, const cplx* const* hV, int K, const cplx* w, int64_t n, cplx* dout) {
+    ProfScope ps(ctx, 6, 8.0 * n * K, 16.0 * n * (K + 1));
     const int nblk = grid_for(ctx, n);
     cplx* partial = ctx->s_dot.c(ctx, (size_t)nblk * MAXV);
     for (int j0 = 0; j0 < K; j0 += MAXV) {
@@ -499,6 +503,7 @@ void bilinear_dot(Ctx* ctx, const cplx* x, const cplx* y, int64_t n, cplx* dout)
 
 void multi_axpy(Ctx* ctx, cplx* w, const cplx* const* hV, const cplx* dcoef, int K, int64_t n,
                 double sign) {
+    ProfScope ps(ctx, 6, 8.0 * n * K, 16.0 * n * (K + 2));
     const int nblk = grid_for(ctx, n);
     for (int j0 = 0; j0 < K; j0 += MAXV) {
         const int kk = std::min(MAXV, K - j0);

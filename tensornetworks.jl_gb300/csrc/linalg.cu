@@ -61,6 +61,71 @@ double* Ctx::pinned(size_t n) {
     return h_pinned;
 }
 
+void ctx_init(Ctx& c, int device) {
+    TN_CHECK_CUDA(cudaSetDevice(device));
+    c.device = device;
+    TN_CHECK_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    TN_CHECK_CUDA(cudaDeviceGetDefaultMemPool(&c.pool, device));
+    uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+    TN_CHECK_CUDA(cudaMemPoolSetAttribute(c.pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    TN_CHECK_SOLVER(cusolverDnCreate(&c.solver));
+    TN_CHECK_SOLVER(cusolverDnSetStream(c.solver, c.stream));
+    TN_CHECK_CUDA(cudaMalloc(&c.d_info, sizeof(int)));
+    TN_CHECK_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
+    TN_CHECK_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
+    TN_CHECK_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
+}
+
+void ctx_release(Ctx& c) {
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    // scratch buffers release through the stream before it goes away
+    Scratch* all[] = {&c.s_gram, &c.s_eigval, &c.s_work, &c.s_x, &c.s_y, &c.s_t1, &c.s_t2,
+                      &c.s_dot, &c.s_coef, &c.s_mixa, &c.s_mixb, &c.s_mixc, &c.s_mixd, &c.s_mixe,
+                      &c.s_mixf};
+    for (Scratch* s : all) s->buf.reset();
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    if (c.solver) cusolverDnDestroy(c.solver);
+    if (c.d_info) cudaFree(c.d_info);
+    if (c.d_err) cudaFree(c.d_err);
+    if (c.h_pinned) cudaFreeHost(c.h_pinned);
+    for (auto& r : c.prof_pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : c.ev_pool) cudaEventDestroy(e);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    c = Ctx{};
+}
+
+cudaEvent_t Ctx::ev_get() {
+    if (!ev_pool.empty()) {
+        cudaEvent_t e = ev_pool.back();
+        ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    TN_CHECK_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void Ctx::prof_flush() {
+    if (prof_pending.empty()) return;
+    TN_CHECK_CUDA(cudaEventSynchronize(prof_pending.back().b));
+    for (ProfRec& r : prof_pending) {
+        float ms = 0.f;
+        TN_CHECK_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        ProfClass& c = prof[r.cls];
+        c.launches += 1;
+        c.ms += ms;
+        c.flops += r.flops;
+        c.bytes += r.bytes;
+        ev_pool.push_back(r.a);
+        ev_pool.push_back(r.b);
+    }
+    prof_pending.clear();
+}
+
 // ---- eigen-decomposition ---------------------------------------------------
 void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam) {
     int lwork = 0;
@@ -70,10 +135,10 @@ void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam) {
                                                 dlam, &lwork));
     cuDoubleComplex* work = static_cast<cuDoubleComplex*>(
         ctx->s_work.get(ctx, sizeof(cuDoubleComplex) * (size_t)std::max(lwork, 1)));
+    ProfScope ps(ctx, 2, 0.0, 16.0 * n * n);
     TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
                                      (int)n, reinterpret_cast<cuDoubleComplex*>(G), (int)n, dlam,
                                      work, lwork, ctx->d_info));
-    ctx->count();
     int info = 0;
     TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();

@@ -168,6 +168,7 @@ void split_natural(Ctx* ctx, const cplx* src, int64_t rows, int64_t K, TcPlanes&
     t.K = K;
     t.ld = tc_ld(K);
     t.p = static_cast<float*>(s.get(ctx, sizeof(float) * t.floats()));
+    ProfScope ps(ctx, 5, 0.0, 16.0 * rows * K + 16.0 * rows * t.ld);
     split_natural_kernel<<<grid_n(ctx, rows * t.ld), 256, 0, ctx->stream>>>(src, rows, K, t.p, t.ld);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
@@ -181,6 +182,7 @@ void split_transpose(Ctx* ctx, const cplx* src, int64_t rows, int64_t K, int64_t
     t.p = static_cast<float*>(s.get(ctx, sizeof(float) * t.floats()));
     TN_REQUIRE((t.ld + 31) / 32 <= 65535, "split_transpose: K too large");
     dim3 grid((unsigned)((rows + 31) / 32), (unsigned)((t.ld + 31) / 32));
+    ProfScope ps(ctx, 5, 0.0, 16.0 * rows * K + 16.0 * rows * t.ld);
     split_transpose_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(src, rows, K, lds, t.p, t.ld);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
@@ -214,6 +216,8 @@ void heff2_planes(Ctx* ctx, MixedWork& B, const cplx* W12, int64_t cl, int64_t c
     const size_t smem = sizeof(float2) * ((size_t)nI * nJ + (size_t)MID_C * MID_A * nJ);
     dim3 grid((unsigned)((cl + MID_A - 1) / MID_A), (unsigned)((cr + MID_C - 1) / MID_C));
     TN_REQUIRE(grid.y <= 65535, "mixed H_eff: chi too large");
+    ProfScope ps(ctx, 4, 8.0 * cl * cr * nI * nJ,
+                 8.0 * (double)S1 * M1 * N1 + 16.0 * (double)t2.rows * t2.K);
     heff_mid_kernel<<<grid, 256, smem, ctx->stream>>>(t1, t1 + (size_t)M1 * N1, S1, chunk1, M1,
                                                       cl, cr, d, (int)wl, (int)wr, W12, t2.p,
                                                       t2.ld, t2.rows);

@@ -350,6 +350,10 @@ int tc_cgemm_partials(Ctx* ctx, const TcPlanes& A, const TcPlanes& B, int64_t M,
     Params p{M, N, K, conjA ? 1 : 0, (int)(kc / BK), out, ldo, plane_stride, chunk_stride,
              err_flag(ctx)};
     dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)S);
+    // algorithmic flops of the complex product (8 per complex multiply-add);
+    // the tensor pipe executes three TF32 passes of them
+    ProfScope ps(ctx, 0, 8.0 * M * N * (double)K,
+                 4.0 * 4.0 * (double)(M + N) * K + 8.0 * M * N * S);
     tc_cgemm_kernel<<<grid, 192, SMEM_BYTES, ctx->stream>>>(ma, mb, p);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
@@ -388,6 +392,7 @@ void tc_reduce_fp64(Ctx* ctx, const float* P, int S, int64_t M, int64_t N, int64
     if (M <= 0 || N <= 0) return;
     int64_t g = (M * N + 255) / 256;
     g = std::min<int64_t>(g, (int64_t)ctx->sm_count * 16);
+    ProfScope ps(ctx, 5, 2.0 * M * N * S, 8.0 * M * N * S + 16.0 * M * N);
     reduce_partials_fp64_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx->stream>>>(
         P, S, M, N, ldp, plane_stride, chunk_stride, out, ldo, accumulate ? 1 : 0);
     ctx->count();

@@ -1,0 +1,284 @@
+"""
+    TensorNetworksGB300
+
+Drop-in GPU backend for the finite-MPS hot path of TensorNetworks.jl.  The
+methods below keep the reference's names, argument types, keywords and return
+values (`dmrg`, `tebd`, `applygates!`, `qjmc_simulation`) and forward the work
+to libtngpu.so through `ccall`.  Model construction (`spinhalf`, `OpList`,
+`MPO(st, H)`, `trotterize`) stays in TensorNetworks.jl; only tensors cross the
+boundary, as column-major `ComplexF64` arrays.
+
+Usage:
+    using TensorNetworks, TensorNetworksGB300
+    psi, energy = TensorNetworksGB300.dmrg(psi, H; maxdim=1024, precision=:mixed)
+"""
+module TensorNetworksGB300
+
+using TensorNetworks
+import TensorNetworks: GMPS, OpList, Sitetypes, GateList
+
+const libtngpu = get(ENV, "TNGPU_LIB", joinpath(@__DIR__, "..", "tngpu", "libtngpu.so"))
+
+const TN_PREC_FP64 = Int32(0)
+const TN_PREC_MIXED = Int32(1)
+
+struct TruncOpts
+    cutoff::Float64
+    maxdim::Int64
+    mindim::Int64
+end
+
+struct DmrgOpts
+    nsites::Int32
+    krylovdim::Int32
+    kryloviter::Int32
+    minsweeps::Int32
+    maxsweeps::Int32
+    tol::Float64
+    tolgrad::Float64
+    numconverges::Float64
+    cutoff::Float64
+    maxdim::Int64
+    mindim::Int64
+    precision::Int32
+    verbose::Int32
+    max_bond_updates::Int32
+    profile_from_sweep::Int32
+end
+
+mutable struct DmrgStats
+    sweeps::Int32
+    maxbonddim::Int32
+    matvecs::Int64
+    seconds::Float64
+    energy_fp64::Float64
+    last_discarded::Float64
+    sweep_cap::Int32
+    sweep_seconds::Ptr{Float64}
+    sweep_energies::Ptr{Float64}
+    sweep_maxdim::Ptr{Int32}
+    bond_updates::Int32
+    bond_cap::Int32
+    bond_seconds::Ptr{Float64}
+    bond_chi::Ptr{Int32}
+end
+DmrgStats() = DmrgStats(0, 0, 0, 0.0, 0.0, 0.0, 0, C_NULL, C_NULL, C_NULL, 0, 0, C_NULL, C_NULL)
+
+mutable struct Context
+    h::Ptr{Cvoid}
+end
+
+const _ctx = Ref{Union{Nothing,Context}}(nothing)
+
+function context(device::Integer=0)
+    if _ctx[] === nothing
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:tn_ctx_create, libtngpu), Int32, (Int32, Ref{Ptr{Cvoid}}), device, h)
+        rc == 0 || error(unsafe_string(ccall((:tn_last_error, libtngpu), Cstring, (Ptr{Cvoid},), C_NULL)))
+        _ctx[] = Context(h[])
+        atexit(() -> ccall((:tn_ctx_destroy, libtngpu), Int32, (Ptr{Cvoid},), _ctx[].h))
+    end
+    return _ctx[]
+end
+
+# The reference raises Julia errors (error("...")); status codes become the same.
+function check(ctx::Context, rc::Integer)
+    rc == 0 && return nothing
+    error(unsafe_string(ccall((:tn_last_error, libtngpu), Cstring, (Ptr{Cvoid},), ctx.h)))
+end
+
+# ---- MPS / MPO transfer ------------------------------------------------------
+function upload(ctx::Context, psi::GMPS)
+    N = length(psi)
+    ts = [convert(Array{ComplexF64,3}, psi[i]) for i = 1:N]
+    dims = Int64[size(ts[1], 1); [size(t, 3) for t in ts]]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve ts begin
+        ptrs = [Ptr{Float64}(pointer(t)) for t in ts]
+        check(ctx, ccall((:tn_mps_upload, libtngpu), Int32,
+                         (Ptr{Cvoid}, Int32, Int32, Ptr{Int64}, Ptr{Ptr{Float64}}, Int32, Ref{Ptr{Cvoid}}),
+                         ctx.h, N, dim(psi), dims, ptrs, center(psi), h))
+    end
+    return h[]
+end
+
+function download!(ctx::Context, psi::GMPS, h::Ptr{Cvoid})
+    N = length(psi)
+    dims = zeros(Int64, N + 1)
+    c = Ref{Int32}(0)
+    check(ctx, ccall((:tn_mps_bonddims, libtngpu), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ref{Int32}),
+                     ctx.h, h, dims, c))
+    ts = [zeros(ComplexF64, dims[i], dim(psi), dims[i+1]) for i = 1:N]
+    GC.@preserve ts begin
+        ptrs = [Ptr{Float64}(pointer(t)) for t in ts]
+        check(ctx, ccall((:tn_mps_download, libtngpu), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Ptr{Float64}}),
+                         ctx.h, h, ptrs))
+    end
+    for i = 1:N
+        psi[i] = ts[i]
+    end
+    psi.center = c[]
+    return psi
+end
+
+destroy_mps(h) = ccall((:tn_mps_destroy, libtngpu), Int32, (Ptr{Cvoid},), h)
+
+function upload_mpo(ctx::Context, H::GMPS)
+    N = length(H)
+    ts = [convert(Array{ComplexF64,4}, H[i]) for i = 1:N]
+    wd = Int64[size(ts[1], 1); [size(t, 4) for t in ts]]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve ts begin
+        ptrs = [Ptr{Float64}(pointer(t)) for t in ts]
+        check(ctx, ccall((:tn_mpo_upload, libtngpu), Int32,
+                         (Ptr{Cvoid}, Int32, Int32, Ptr{Int64}, Ptr{Ptr{Float64}}, Ref{Ptr{Cvoid}}),
+                         ctx.h, N, dim(H), wd, ptrs, h))
+    end
+    return h[]
+end
+
+# ---- dmrg (src/algorithms/mps/dmrg.jl:128-154) -------------------------------
+function dmrg(psi::GMPS, H::GMPS; nsites::Int=2, krylovdim::Int=3, kryloviter::Int=2,
+              minsweeps::Int=1, maxsweeps::Int=1000, tol::Float64=1e-10, tolgrad::Float64=1e-5,
+              numconverges::Real=4, cutoff::Float64=1e-12, maxdim::Int=1000, mindim::Int=1,
+              verbose::Bool=true, precision::Symbol=:fp64, kwargs...)
+    rank(psi) != 1 && error("Psi must be a GMPS of rank 1 (vector).")
+    (length(H) != length(psi) || dim(H) != dim(psi)) && error("GMPS must share the same properties.")
+    ctx = context()
+    hpsi = upload(ctx, psi)
+    hH = upload_mpo(ctx, H)
+    opts = DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
+                    Float64(numconverges), cutoff, maxdim, mindim,
+                    precision === :mixed ? TN_PREC_MIXED : TN_PREC_FP64, verbose, 0, -1)
+    energy = Ref{Float64}(0.0)
+    stats = Ref(DmrgStats())
+    try
+        check(ctx, ccall((:tn_dmrg, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{DmrgOpts}, Ref{Float64}, Ref{DmrgStats}),
+                         ctx.h, hpsi, hH, opts, energy, stats))
+        download!(ctx, psi, hpsi)
+    finally
+        destroy_mps(hpsi)
+        ccall((:tn_mpo_destroy, libtngpu), Int32, (Ptr{Cvoid},), hH)
+    end
+    return psi, energy[]
+end
+
+# ---- gates, applygates!, tebd (gatelist.jl:191-227, tebd.jl:3-100) -----------
+function upload_gates(ctx::Context, gl::GateList, d::Integer)
+    rows = length(gl.gates)
+    row_len = Int32[length(r) for r in gl.gates]
+    sites = Int32[s for r in gl.sites for s in r]
+    gs = [convert(Array{ComplexF64}, g) for r in gl.gates for g in r]
+    ns = Int32[ndims(g) ÷ 2 for g in gs]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve gs begin
+        ptrs = [Ptr{Float64}(pointer(g)) for g in gs]
+        check(ctx, ccall((:tn_gates_upload, libtngpu), Int32,
+                         (Ptr{Cvoid}, Int32, Int32, Int32, Ptr{Int32}, Ptr{Int32}, Ptr{Int32},
+                          Ptr{Ptr{Float64}}, Ref{Ptr{Cvoid}}),
+                         ctx.h, length(gl), d, rows, row_len, sites, ns, ptrs, h))
+    end
+    return h[]
+end
+
+function applygates!(psi::GMPS, gates::GateList; cutoff::Real=0.0, maxdim::Int=0, mindim::Int=1, kwargs...)
+    ctx = context()
+    hpsi = upload(ctx, psi)
+    hg = upload_gates(ctx, gates, dim(psi))
+    t = TruncOpts(cutoff, maxdim, mindim)
+    try
+        check(ctx, ccall((:tn_applygates, libtngpu), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{TruncOpts}),
+                         ctx.h, hpsi, hg, t))
+        download!(ctx, psi, hpsi)
+    finally
+        destroy_mps(hpsi)
+        ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
+    end
+    return 1
+end
+
+function tebd(st::Sitetypes, psi::GMPS, H::OpList, dt::Number, tmax::Number, save::Number,
+              observers::Vector=[]; cutoff::Float64=1e-12, maxdim::Int=0, mindim::Int=1,
+              evol::String="imag", order::Int=2, norm::Real=0.0, kwargs...)
+    st.dim != dim(psi) && error("Sitetypes and MPS physical dimensions do not match.")
+    length(psi) != length(H) && error("OpList and MPS have different lengths.")
+    gates = trotterize(st, H, dt; evol=evol, order=order)
+    nsteps = Int(round(tmax / dt))
+    save = save < dt ? dt : save
+    nsave = Int(round(save / dt))
+    normal = Float64(norm)
+    energy = real(sum(inner(st, psi, H, psi)))
+    for observer in observers
+        TensorNetworks.measure!(observer, 0.0, psi, normal, energy)
+    end
+    ctx = context()
+    TensorNetworks.norm(psi)
+    hpsi = upload(ctx, psi)
+    hg = upload_gates(ctx, gates, dim(psi))
+    t = TruncOpts(cutoff, maxdim, mindim)
+    step = 0
+    converged = false
+    try
+        while !converged
+            ln = Ref{Float64}(0.0)
+            check(ctx, ccall((:tn_tebd_steps, libtngpu), Int32,
+                             (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ref{TruncOpts}, Ref{Float64}),
+                             ctx.h, hpsi, hg, 1, t, ln))
+            normal += ln[]
+            step += 1
+            converged = step >= nsteps
+            if step % nsave == 0
+                download!(ctx, psi, hpsi)
+                energy = real(sum(inner(st, psi, H, psi)))
+                for observer in observers
+                    TensorNetworks.measure!(observer, step * dt, psi, normal, energy)
+                    converged = converged || TensorNetworks.checkdone!(observer)
+                end
+            end
+        end
+        download!(ctx, psi, hpsi)
+    finally
+        destroy_mps(hpsi)
+        ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
+    end
+    return psi, energy
+end
+
+# ---- qjmc_simulation (qjmc.jl:28-166), one trajectory, explicit draws --------
+function qjmc_simulation(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, tmax::Real, dt::Real,
+                         observers=[]; save::Real=0, cutoff::Real=1e-12, mindim::Int=1, maxdim::Int=0,
+                         draws::Vector{Float64}=rand(3 * (ceil(Int, tmax / dt) + 1)), kwargs...)
+    save = save == 0 ? dt : save
+    steps = Int(ceil(round(tmax / dt, digits=5)))
+    savesteps = Int(ceil(round(save / dt)))
+    escapeops, gates = TensorNetworks.qjmc_gates(st, H, jumpops, dt)
+    all(length(s) == 1 for s in jumpops.sites) || error("multi-site jump operators are not on this path")
+    ctx = context()
+    hpsi = upload(ctx, psi)
+    hg = upload_gates(ctx, gates, dim(psi))
+    jsites = Int32[s[1] for s in jumpops.sites]
+    jops = reduce(vcat, [vec(op(st, o[1])) for o in jumpops.ops])
+    jco = ComplexF64.(jumpops.coeffs)
+    cap = steps + 1
+    jumps = zeros(Int32, cap)
+    jtimes = zeros(Float64, cap)
+    nj = Ref{Int32}(cap)
+    used = Ref{Int64}(0)
+    t = TruncOpts(cutoff, maxdim, mindim)
+    try
+        check(ctx, ccall((:tn_qjmc_run, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{ComplexF64}, Ptr{ComplexF64},
+                          Int32, Float64, Ptr{Float64}, Int64, Ref{TruncOpts}, Int32, Int32, Ptr{Int32},
+                          Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Int32}, Ptr{Float64}, Ref{Int32}, Ref{Int64}),
+                         ctx.h, hpsi, hg, length(jsites), jsites, jops, jco, steps, dt, draws, length(draws),
+                         t, savesteps, 0, C_NULL, C_NULL, C_NULL, jumps, jtimes, nj, used))
+        download!(ctx, psi, hpsi)
+    finally
+        destroy_mps(hpsi)
+        ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
+    end
+    return Int.(jumps[1:nj[]]), jtimes[1:nj[]]
+end
+
+end # module

@@ -35,14 +35,14 @@ class DmrgOpts(C.Structure):
     _fields_ = [("nsites", i32), ("krylovdim", i32), ("kryloviter", i32), ("minsweeps", i32),
                 ("maxsweeps", i32), ("tol", f64), ("tolgrad", f64), ("numconverges", f64),
                 ("cutoff", f64), ("maxdim", i64), ("mindim", i64), ("precision", i32),
-                ("verbose", i32), ("max_bond_updates", i32)]
+                ("verbose", i32), ("max_bond_updates", i32), ("profile_from_sweep", i32)]
 
 
 class DmrgStats(C.Structure):
     _fields_ = [("sweeps", i32), ("maxbonddim", i32), ("matvecs", i64), ("seconds", f64),
                 ("energy_fp64", f64), ("last_discarded", f64), ("sweep_cap", i32),
                 ("sweep_seconds", dp), ("sweep_energies", dp), ("sweep_maxdim", i32p),
-                ("bond_updates", i32)]
+                ("bond_updates", i32), ("bond_cap", i32), ("bond_seconds", dp), ("bond_chi", i32p)]
 
 
 _SIGS = {
@@ -73,13 +73,23 @@ _SIGS = {
     "tn_qjmc_rates": (i32, [P, P, i32, i32p, dp, dp, dp]),
     "tn_qjmc_run": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, dp, i64, C.POINTER(TruncOpts),
                           i32, i32, i32p, dp, dp, i32p, dp, i32p, i64p]),
+    "tn_qjmc_batch": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, i32, dp, i64,
+                            C.POINTER(TruncOpts), i32, i32, i32p, dp, dp, i32p, i32]),
     "tn_heff2_apply": (i32, [P, i64, i64, i32, i64, i64, i64, dp, dp, dp, dp, dp, dp, i32]),
     "tn_env_left": (i32, [P, i64, i64, i32, i64, i64, dp, dp, dp, dp, i32]),
     "tn_env_right": (i32, [P, i64, i64, i32, i64, i64, dp, dp, dp, dp, i32]),
     "tn_gate2_apply": (i32, [P, i64, i64, i64, i32, dp, dp, dp, dp]),
     "tn_truncate": (i32, [P, i64, i64, dp, C.POINTER(TruncOpts), i32, dp, dp, dp, i64p]),
     "tn_gemm": (i32, [P, i64, i64, i64, dp, i32, dp, dp, i32]),
+    "tn_profile_enable": (i32, [P, i32]),
+    "tn_profile_reset": (i32, [P]),
+    "tn_profile_read": (i32, [P, i64p, dp, dp, dp]),
 }
+
+PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "zheevd (cuSOLVER FP64)",
+                "small_apply_kernel (FP64 legs)", "heff_mid_kernel (FP32 leg)",
+                "operand conversion / partial reduction", "Lanczos vector ops",
+                "all launches (count only)")
 
 EXPORTED = tuple(_SIGS)
 

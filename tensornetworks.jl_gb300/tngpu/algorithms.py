@@ -23,7 +23,8 @@ from .mps import GMPS, MPOHandle, inner
 # ---------------------------------------------------------------------------
 def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
          maxsweeps=1000, tol=1e-10, tolgrad=1e-5, numconverges=4, cutoff=1e-12, maxdim=1000,
-         mindim=1, verbose=True, precision="fp64", stats=None, max_bond_updates=0):
+         mindim=1, verbose=True, precision="fp64", stats=None, max_bond_updates=0,
+         profile_from_sweep=-1):
     """Two-site DMRG; mutates ``psi`` and returns (psi, energy).
 
     ``stats`` (a dict) receives sweeps, matvecs, per-sweep device seconds and
@@ -37,7 +38,7 @@ def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps
         raise ValueError("only two-site DMRG (nsites=2) is on this path")
     o = L.DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
                    float(numconverges), cutoff, maxdim, mindim, L.PREC[precision], int(bool(verbose)),
-                   int(max_bond_updates))
+                   int(max_bond_updates), int(profile_from_sweep))
     e = C.c_double()
     st = L.DmrgStats()
     cap = maxsweeps if maxsweeps > 0 else 1000
@@ -46,6 +47,11 @@ def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps
     st.sweep_cap = cap
     st.sweep_seconds, st.sweep_energies = L.as_dp(secs), L.as_dp(ens)
     st.sweep_maxdim = mds.ctypes.data_as(L.i32p)
+    bcap = max(1, (len(psi) - 1) * min(cap, 64))
+    bsec = np.zeros(bcap)
+    bchi = np.zeros(bcap, dtype=np.int32)
+    st.bond_cap = bcap
+    st.bond_seconds, st.bond_chi = L.as_dp(bsec), bchi.ctypes.data_as(L.i32p)
     ctx = psi.ctx
     ctx.check(ctx.lib.tn_dmrg(ctx.h, psi._h, H._h, C.byref(o), C.byref(e), C.byref(st)))
     if stats is not None:
@@ -54,7 +60,9 @@ def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps
                      last_discarded=st.last_discarded, bond_updates=st.bond_updates,
                      sweep_seconds=secs[: min(st.sweeps, cap)].tolist(),
                      sweep_energies=ens[: min(st.sweeps, cap)].tolist(),
-                     sweep_maxdim=mds[: min(st.sweeps, cap)].tolist())
+                     sweep_maxdim=mds[: min(st.sweeps, cap)].tolist(),
+                     bond_seconds=bsec[: min(st.bond_updates, bcap)].tolist(),
+                     bond_chi=bchi[: min(st.bond_updates, bcap)].tolist())
     return psi, e.value
 
 
@@ -211,6 +219,50 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
         esc.add([st.opprod([st.dag(o), o]) for o in ops], sites, c ** 2)
     heff = (-1j) * H + (-0.5) * esc
     return heff, trotter_rows(st, heff, dt, **kw)
+
+
+def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
+                  draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=16):
+    """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
+    (left unchanged), advanced concurrently on the GPU.  Returns (times,
+    averaged single-site observables [rows x terms], jump counts).  ``draws``
+    is an (ntraj x m) array of uniforms consumed per trajectory in the
+    reference's order; otherwise they come from ``rand``."""
+    save = dt if save == 0 else save
+    steps = math.ceil(round(tmax / dt, 5))
+    savesteps = math.ceil(round(save / dt))
+    _, rows = qjmc_gates(st, H, jumpops, dt)
+    gates = GateList(H.length, rows, st.dim, psi.ctx)
+    if any(len(s) != 1 for s in jumpops.sites) or any(len(s) != 1 for s in obs.sites):
+        raise NotImplementedError("single-site jump operators and observables only")
+    if draws is None:
+        g = rand if rand is not None else np.random.default_rng()
+        draws = g.random((ntraj, 3 * steps + 3))
+    draws = np.ascontiguousarray(draws, dtype=np.float64)
+    if draws.shape[0] != ntraj:
+        raise ValueError("draws must have one row per trajectory")
+    jsites = np.asarray([s[0] for s in jumpops.sites], dtype=np.int32)
+    jops = np.concatenate([L.cplx_f(st.op(o[0])).ravel(order="F") for o in jumpops.ops]).astype(np.complex128)
+    jco = np.asarray(jumpops.coeffs, dtype=np.complex128)
+    osites = np.asarray([s[0] for s in obs.sites], dtype=np.int32)
+    oops = np.concatenate([L.cplx_f(complex(c) * st.op(o[0])).ravel(order="F")
+                           for o, c in zip(obs.ops, obs.coeffs)]).astype(np.complex128)
+    nrows = steps // savesteps + 1
+    out = np.zeros((nrows, len(osites)), dtype=np.complex128)
+    nj = np.zeros(ntraj, dtype=np.int32)
+    t = L.trunc(cutoff, maxdim, mindim)
+    ctx = psi.ctx
+    ctx.check(ctx.lib.tn_qjmc_batch(
+        ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
+        L.as_dp(jco), steps, float(dt), ntraj, L.as_dp(draws), draws.shape[1], C.byref(t), savesteps,
+        len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
+        nj.ctypes.data_as(L.i32p), int(workers)))
+    tt, times = 0.0, [0.0]
+    for i in range(1, steps + 1):
+        tt += dt
+        if i % savesteps == 0:
+            times.append(tt)
+    return times, out, nj
 
 
 class QJMCOperators:

@@ -343,3 +343,34 @@ def test_error_status_on_bad_input(tn):
     # the context stays usable after an error
     pg.movecenter(2)
     assert pg.center == 2
+
+
+def test_qjmc_ensemble_matches_per_trajectory_oracle(tn):
+    """Concurrent trajectories (3 workers) against the oracle run trajectory
+    by trajectory on the same draw rows: averaged <Z_i>(t) and jump counts."""
+    N, dt, steps, ntraj = 6, 0.05, 30, 6
+    draws = np.random.default_rng(9).random((ntraj, 3 * steps + 3))
+    Ho, Lo = ising_qjmc(O, N)
+    zo = O.OpList(N)
+    for i in range(1, N + 1):
+        zo.add("z", i)
+    avg, counts = 0.0, []
+    for t in range(ntraj):
+        po = O.product_mps(O.spinhalf(), ["up"] * N)
+        rec = {}
+        j, _ = O.qjmc_simulation(O.spinhalf(), po, Ho, Lo, steps * dt, dt,
+                                 O.algorithms.UniformStream(draws[t]), [zo], save=5 * dt,
+                                 cutoff=1e-10, maxdim=16, record=rec)
+        avg = avg + np.real(np.array([r[0] for r in rec["ops"]]))
+        counts.append(len(j))
+    avg /= ntraj
+    Hg, Lg = ising_qjmc(tn, N)
+    zg = tn.OpList(N)
+    for i in range(1, N + 1):
+        zg.add("z", i)
+    pg = tn.productMPS(tn.spinhalf(), ["up"] * N)
+    times, out, nj = tn.qjmc_ensemble(tn.spinhalf(), pg, Hg, Lg, steps * dt, dt, zg, ntraj,
+                                      draws=draws, save=5 * dt, cutoff=1e-10, maxdim=16, workers=3)
+    assert list(nj) == counts and sum(counts) > 0
+    assert out.shape == avg.shape and np.allclose(np.real(out), avg, atol=1e-9)
+    assert len(times) == out.shape[0]
