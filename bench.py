@@ -51,12 +51,14 @@ def parse():
     p.add_argument("--chi", type=int, default=CHI)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-side", action="store_true", help="skip the QJMC and TEBD samples")
     return p.parse_args()
 
 
 def config(args):
-    return {"workload": f"XXZ chain N={args.n} J=Delta=1 OBC, two-site DMRG at maxdim={args.chi} "
-                        f"after a 64/256 ramp, cutoff 1e-12, krylovdim 3, kryloviter 2",
+    return {"workload": f"XXZ chain N={args.n} J=Delta=1 OBC, two-site DMRG at chi={args.chi} "
+                        f"(maxdim=mindim={args.chi}; the 1e-12 cutoff alone settles near chi 220 "
+                        f"for this chain) after a 64/256 ramp, cutoff 1e-12, krylovdim 3, kryloviter 2",
             "model": "Heisenberg XXZ MPO (w=5)", "n_sites": args.n, "chi": args.chi,
             "initial_state": f"random MPS D={D0}, numpy PCG64 seed {SEED}",
             "l2": "working set > L2 (MPS 2.7 GB, environments up to 80 MB each); no flush",
@@ -210,16 +212,20 @@ def ours(args):
     st = {}
     t0 = time.perf_counter()
     # an even number of directional sweeps leaves the centre at site 1, so the
-    # FP64 sample and the end-to-end run start without re-canonicalising
-    total = Wu + K + (Wu + K) % 2
-    _, E = tn.dmrg(psi, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=total, maxsweeps=total,
+    # FP64 sample and the end-to-end run start without re-canonicalising; a
+    # padding sweep joins the warm-ups so the timed sweeps are the last K
+    pad = (Wu + K) % 2
+    Wu_eff = Wu + pad
+    total = Wu_eff + K
+    _, E = tn.dmrg(psi, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=total,
+                   maxsweeps=total,
                    numconverges=np.inf, verbose=False, precision="mixed", stats=st,
-                   profile_from_sweep=Wu)
+                   profile_from_sweep=Wu_eff)
     wall_main = time.perf_counter() - t0
     clocks = clk.stop()
     log(f"main: {wall_main:.1f} s, sweeps {['%.2f' % s for s in st['sweep_seconds']]}, "
         f"maxdim {st['sweep_maxdim']}, E={E:.12f}, E64={st['energy_fp64']:.12f}, ramp {ramp}")
-    timed = st["sweep_seconds"][Wu:Wu + K]
+    timed = st["sweep_seconds"][Wu_eff:Wu_eff + K]
     t_timed = float(sum(timed))
     if dist:
         import torch
@@ -282,6 +288,17 @@ def ours(args):
     if not args.no_e2e:
         line["e2e"] = e2e_run(tn, ctx, psi, W_mpo, args, world)
         log("e2e: " + json.dumps(line["e2e"]))
+    if rank == 0 and not args.no_side:
+        try:
+            line["qjmc"] = qjmc_sample(tn, ctx)
+            log("qjmc: " + json.dumps(line["qjmc"]))
+        except Exception as e:  # a side measurement never voids the headline line
+            line["qjmc"] = {"error": str(e)}
+        try:
+            line["tebd"] = tebd_sample(tn, ctx)
+            log("tebd: " + json.dumps(line["tebd"]))
+        except Exception as e:
+            line["tebd"] = {"error": str(e)}
     if rank == 0 and not args.no_cpu:
         t = cpu_bond_sample(args.chi)
         line["cpu_baseline"] = {"value": 1.0 / (t * (args.n - 1)), "unit": UNIT,
@@ -294,6 +311,79 @@ def ours(args):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=64, workers=16):
+    """BASELINE config 4 shapes: N=32 Ising chain H = sum Z Z + 0.8 sum X, jumps
+    L_i = sqrt(0.1) s-_i, all-up start, dt=0.01, maxdim 64, cutoff 1e-10.  One
+    trajectory is evolved `pre_steps` (untimed) so the timed steps run at grown
+    bond dimension; from it, `steps` steps of one trajectory alone and of
+    `ntraj` trajectories on `workers` concurrent streams are timed."""
+    N, dt = 32, 0.01
+    H, Lj, Z = tn.OpList(N), tn.OpList(N), tn.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], 1.0)
+    for i in range(1, N + 1):
+        H.add("x", i, 0.8)
+        Lj.add("s-", i, np.sqrt(0.1))
+        Z.add("z", i)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up"] * N, ctx=ctx)
+    rng = np.random.default_rng(4)
+    t0 = time.perf_counter()
+    tn.qjmc_simulation(st, psi, H, Lj, pre_steps * dt, dt, [], cutoff=1e-10, maxdim=64,
+                       draws=rng.random(3 * pre_steps + 3))
+    pre_s = time.perf_counter() - t0
+    chi = psi.maxbonddim()
+    seeds = np.random.SeedSequence(4).spawn(ntraj)
+    draws = np.stack([np.random.default_rng(s).random(3 * steps + 3) for s in seeds])
+    t0 = time.perf_counter()
+    tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 1, draws=draws[:1], cutoff=1e-10,
+                     maxdim=64, workers=1)
+    single = steps / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    _, zav, nj = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, draws=draws,
+                                  cutoff=1e-10, maxdim=64, workers=workers)
+    batched = ntraj * steps / (time.perf_counter() - t0)
+    return {"traj_steps_per_s_single": single, "traj_steps_per_s_batched": batched,
+            "batched_vs_single": batched / single, "start_chi": chi, "pre_steps_s": pre_s,
+            "jumps_in_sample": int(nj.sum()), "z_avg_final": float(np.real(zav[-1]).mean()),
+            "sample": f"{ntraj} trajectories x {steps} steps on {workers} streams vs 1 x {steps}, "
+                      f"from a state evolved {pre_steps} steps (chi {chi}); N=32, dt=0.01, maxdim 64"}
+
+
+def tebd_sample(tn, ctx, pre_steps=20, steps=4):
+    """BASELINE config 3 shapes: N=64 XXZ (J=1, Delta=0.5) + staggered field
+    0.2(-1)^i, Neel start, real time, 2nd order, dt=0.05, maxdim 256, cutoff
+    1e-10; `steps` timed TEBD steps after `pre_steps` untimed ones."""
+    import ctypes as C
+
+    from tngpu import _lib as L
+    N, dt = 64, 0.05
+    H = tn.OpList(N)
+    for i in range(1, N):
+        H.add(["x", "x"], [i, i + 1], 1.0)
+        H.add(["y", "y"], [i, i + 1], 1.0)
+        H.add(["z", "z"], [i, i + 1], 0.5)
+    for i in range(1, N + 1):
+        H.add("z", i, 0.2 * (-1) ** i)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
+    gates = tn.trotterize(st, H, dt, order=2, evol="real", ctx=ctx)
+    psi.norm()
+    t = L.trunc(1e-10, 256, 1)
+    ln = C.c_double(0.0)
+    t0 = time.perf_counter()
+    ctx.check(ctx.lib.tn_tebd_steps(ctx.h, psi._h, gates._h, pre_steps, C.byref(t), C.byref(ln)))
+    pre_s = time.perf_counter() - t0
+    chi0 = psi.maxbonddim()
+    t0 = time.perf_counter()
+    ctx.check(ctx.lib.tn_tebd_steps(ctx.h, psi._h, gates._h, steps, C.byref(t), C.byref(ln)))
+    dt_s = time.perf_counter() - t0
+    return {"steps_per_s": steps / dt_s, "chi_start": chi0, "chi_end": psi.maxbonddim(),
+            "pre_steps_s": pre_s,
+            "sample": f"{steps} steps after {pre_steps} untimed (t={pre_steps * dt:.2f}); N=64, "
+                      "dt=0.05, maxdim 256, cutoff 1e-10, 3 gate rows per step"}
 
 
 def cublas_zgemm_tflops(device):
@@ -315,22 +405,24 @@ def cublas_zgemm_tflops(device):
 
 
 def fp64_sample(tn, psi, W_mpo, args, st_mixed, nbonds=14):
-    """Plain FP64 DMRG bond updates from the chi=1024 state (the first
-    `nbonds` of a right sweep, which reach the bulk chi); the FP64 sweep time
-    is estimated from the bulk per-bond time scaled by each bond's chi^3."""
+    """Plain FP64 DMRG bond updates from the chi=1024 state: the first
+    `nbonds` of a right sweep (the last of them at the bulk chi).  The FP64
+    sweep time is the measured time of those bonds plus, for every other
+    bond, the bulk per-bond time scaled by (chi_bond / chi_bulk)^3."""
     p = psi.copy()
     st = {}
-    tn.dmrg(p, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=1, maxsweeps=1, numconverges=np.inf,
-            verbose=False, precision="fp64", stats=st, max_bond_updates=nbonds)
+    tn.dmrg(p, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=1, maxsweeps=1,
+            numconverges=np.inf, verbose=False, precision="fp64", stats=st, max_bond_updates=nbonds)
     secs, chis = np.asarray(st["bond_seconds"]), np.asarray(st["bond_chi"])
     bulk = secs[chis == chis.max()]
     per_bulk = float(bulk[1:].mean() if bulk.size > 1 else bulk.mean())
-    dims = p.bonddims()
+    dims = psi.bonddims()
     chi_b = [max(dims[i], dims[i + 2]) for i in range(len(dims) - 2)]
-    est = sum(per_bulk * (c / chis.max()) ** 3 for c in chi_b)
+    est = float(secs.sum()) + sum(per_bulk * (c / chis.max()) ** 3 for c in chi_b[len(secs):])
     return {"bond_seconds": secs.tolist(), "bond_chi": chis.tolist(), "bulk_bond_s": per_bulk,
-            "sweep_s_est": est, "sweeps_per_s_est": 1.0 / est,
-            "method": f"{nbonds} FP64 bond updates; sweep = sum over bonds of the bulk time x (chi/chi_max)^3"}
+            "bulk_chi": int(chis.max()), "sweep_s_est": est, "sweeps_per_s_est": 1.0 / est,
+            "method": f"{nbonds} FP64 bond updates measured; remaining bonds = bulk time x "
+                      "(chi/chi_bulk)^3"}
 
 
 def e2e_run(tn, ctx, psi, W_mpo, args, world):
@@ -355,7 +447,8 @@ def e2e_run(tn, ctx, psi, W_mpo, args, world):
     h = C.c_void_p()
     ctx.check(ctx.lib.tn_mps_upload(ctx.h, len(ts), 2, dims, L.ptr_array(views), psi.center, C.byref(h)))
     g = tn.GMPS(h, len(ts), 2, ctx)
-    tn.dmrg(g, W_mpo, maxdim=args.chi, cutoff=1e-12, minsweeps=K, maxsweeps=K, numconverges=np.inf,
+    tn.dmrg(g, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=K, maxsweeps=K,
+            numconverges=np.inf,
             verbose=False, precision="mixed")
     out = g.bonddims()
     outs = []
