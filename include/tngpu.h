@@ -200,6 +200,22 @@ int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, in
 int32_t tn_heff2_apply(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl, int64_t wm,
                        int64_t wr, const double* L, const double* W1, const double* W2,
                        const double* R, const double* theta, double* out, int32_t precision);
+/* The same product as tn_heff2_apply (FP64) for callers that cannot allocate
+ * device memory: hosts that run inside a device-memory budget of their own
+ * and hand the library buffers from their arena, or loops where an
+ * allocation's implicit synchronisation is not allowed.  Every pointer
+ * (L, W1, W2, R, theta, out) is a DEVICE pointer the caller owns; nothing is
+ * allocated.  Intermediates live in one static 64 MiB device array that the
+ * library holds on every GPU that loads it, until exit; problems needing
+ * more (16*chil*chir*d^2*(wl+wr) bytes plus the merged operator) are
+ * rejected with TN_ERR_INVALID.  All calls share that array: calls whose GPU
+ * work overlaps race and must be serialised by the caller.  The first call on
+ * a device resolves the array's address; make it before any stream capture.
+ * No counterpart in the reference: an addition for allocation-free callers. */
+int32_t tn_heff2_apply_noalloc(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl,
+                               int64_t wm, int64_t wr, const double* L, const double* W1,
+                               const double* W2, const double* R, const double* theta,
+                               double* out);
 /* L'[a',w',b'] = sum L[a,w,b] conj(A[a,s',a']) W[w,s',s,w'] A[b,s,b'] (projmps.jl:50-66). */
 int32_t tn_env_left(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl, int64_t wr,
                     const double* L, const double* A, const double* W, double* out, int32_t precision);

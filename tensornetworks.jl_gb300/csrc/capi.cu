@@ -28,6 +28,9 @@ void mixed_unit_heff2(Ctx* ctx, const cplx* L, const cplx* W12, const cplx* R, i
                       int64_t cr, int d, int64_t wl, int64_t wr, const cplx* x, cplx* y);
 void mixed_gemm(Ctx* ctx, int64_t m, int64_t n, int64_t k, const cplx* A, bool conj_a,
                 const cplx* B, cplx* C);
+void heff2_noalloc(Ctx* ctx, int64_t cl, int64_t cr, int d, int64_t wl, int64_t wm, int64_t wr,
+                   const cplx* L, const cplx* W1, const cplx* W2, const cplx* R, const cplx* theta,
+                   cplx* out);
 void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsites,
                 const double* jops, const double* jcoeffs, int nsteps, double dt, int ntraj,
                 const double* draws, int64_t ndraws_per_traj, const Trunc& t, int save_every,
@@ -601,6 +604,19 @@ int32_t tn_heff2_apply(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl,
         d2h(ctx, out, dO.p, 16 * nT);
         ctx->sync();
     }
+    TN_API_END
+}
+
+int32_t tn_heff2_apply_noalloc(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl,
+                               int64_t wm, int64_t wr, const double* L, const double* W1,
+                               const double* W2, const double* R, const double* theta,
+                               double* out) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h && L && W1 && W2 && R && theta && out, "null argument");
+    heff2_noalloc(&h->c, cl, cr, d, wl, wm, wr, reinterpret_cast<const cplx*>(L),
+                  reinterpret_cast<const cplx*>(W1), reinterpret_cast<const cplx*>(W2),
+                  reinterpret_cast<const cplx*>(R), reinterpret_cast<const cplx*>(theta),
+                  reinterpret_cast<cplx*>(out));
     TN_API_END
 }
 
