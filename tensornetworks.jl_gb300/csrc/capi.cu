@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "mixed.cuh"
 #include "mps.cuh"
 
 namespace tn {
@@ -644,7 +645,7 @@ int32_t tn_env_left(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl, in
                     const double* L, const double* A, const double* W, double* out, int32_t precision) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(L && A && W && out, "null argument");
-    TN_REQUIRE(precision == TN_PREC_FP64, "environment updates on host buffers run in FP64");
+    TN_REQUIRE(precision == TN_PREC_FP64 || precision == TN_PREC_MIXED, "unknown precision");
     Ctx* ctx = &h->c;
     tn_mpo H1;
     H1.ctx = ctx;
@@ -660,7 +661,12 @@ int32_t tn_env_left(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl, in
     DBuf dL(ctx, 16 * nL), dA(ctx, 16 * nA), dO(ctx, 16 * nO);
     h2d(ctx, dL.p, L, 16 * nL);
     h2d(ctx, dA.p, A, 16 * nA);
-    env_left(ctx, dL.c(), cl, wl, cl, dA.c(), cr, &H1, 1, dA.c(), cr, d, dO.c());
+    if (precision == TN_PREC_MIXED) {
+        mixed_env_left(ctx, dL.c(), cl, wl, cl, dA.c(), cr, H1.Ml[0].c(), d, wr, dA.c(), cr, dO.c());
+        tc_check_error(ctx);
+    } else {
+        env_left(ctx, dL.c(), cl, wl, cl, dA.c(), cr, &H1, 1, dA.c(), cr, d, dO.c());
+    }
     d2h(ctx, out, dO.p, 16 * nO);
     ctx->sync();
     TN_API_END
@@ -670,7 +676,7 @@ int32_t tn_env_right(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl, i
                      const double* R, const double* A, const double* W, double* out, int32_t precision) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(R && A && W && out, "null argument");
-    TN_REQUIRE(precision == TN_PREC_FP64, "environment updates on host buffers run in FP64");
+    TN_REQUIRE(precision == TN_PREC_FP64 || precision == TN_PREC_MIXED, "unknown precision");
     Ctx* ctx = &h->c;
     tn_mpo H1;
     H1.ctx = ctx;
@@ -686,7 +692,12 @@ int32_t tn_env_right(tn_ctx* h, int64_t cl, int64_t cr, int32_t d, int64_t wl, i
     DBuf dR(ctx, 16 * nR), dA(ctx, 16 * nA), dO(ctx, 16 * nO);
     h2d(ctx, dR.p, R, 16 * nR);
     h2d(ctx, dA.p, A, 16 * nA);
-    env_right(ctx, dR.c(), cr, wr, cr, dA.c(), cl, &H1, 1, dA.c(), cl, d, dO.c());
+    if (precision == TN_PREC_MIXED) {
+        mixed_env_right(ctx, dR.c(), cr, wr, cr, dA.c(), cl, H1.Mr[0].c(), d, wl, dA.c(), cl, dO.c());
+        tc_check_error(ctx);
+    } else {
+        env_right(ctx, dR.c(), cr, wr, cr, dA.c(), cl, &H1, 1, dA.c(), cl, d, dO.c());
+    }
     d2h(ctx, out, dO.p, 16 * nO);
     ctx->sync();
     TN_API_END

@@ -83,6 +83,9 @@ struct Ctx {
         s_mixd, s_mixe, s_mixf;
     int* d_info = nullptr;
     int* d_err = nullptr;  // set by device code when a bounded wait runs out
+    // mixed precision on: environment updates and truncation projections run
+    // on the tensor cores (set for the duration of a mixed-precision sweep)
+    bool mixed = false;
     double* h_pinned = nullptr;  // small pinned staging area
     size_t h_pinned_n = 0;
     // kernel profiler: CUDA events around launches, per class
@@ -154,7 +157,7 @@ enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };  // R: conjugate without tra
 // C[m x n] = alpha * op(A) * op(B) + beta * C, column-major, batched by count.
 void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha, const cplx* A,
            int64_t lda, int64_t strideA, const cplx* B, int64_t ldb, int64_t strideB, cplx beta,
-           cplx* C, int64_t ldc, int64_t strideC, int64_t batch = 1);
+           cplx* C, int64_t ldc, int64_t strideC, int64_t batch = 1, bool lower_only = false);
 
 // out[a + lda_o*J + ldc_o*c] (=|+=) sum_I in[a + lda_i*I + ldc_i*c] * M[I + nI*J]
 void small_apply(Ctx* ctx, const cplx* in, cplx* out, const cplx* M, int nI, int nJ, int64_t na,

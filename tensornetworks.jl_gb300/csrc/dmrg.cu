@@ -217,7 +217,11 @@ struct EnvCache {
         const cplx* L = block(i - 1, la, lw, lb);
         const int64_t na = psi->dr(i), nw = H->w[i], nb = psi->dr(i);
         DBuf out(ctx, sizeof(cplx) * na * nw * nb);
-        env_left(ctx, L, la, lw, lb, psi->site(i), na, H, i, psi->site(i), nb, psi->d, out.c());
+        if (ctx->mixed)
+            mixed_env_left(ctx, L, la, lw, lb, psi->site(i), na, H->Ml[i - 1].c(), psi->d, nw,
+                           psi->site(i), nb, out.c());
+        else
+            env_left(ctx, L, la, lw, lb, psi->site(i), na, H, i, psi->site(i), nb, psi->d, out.c());
         blk[i] = std::move(out);
         a[i] = na;
         w[i] = nw;
@@ -228,7 +232,11 @@ struct EnvCache {
         const cplx* R = block(i + 1, ra, rw, rb);
         const int64_t na = psi->dl(i), nw = H->w[i - 1], nb = psi->dl(i);
         DBuf out(ctx, sizeof(cplx) * na * nw * nb);
-        env_right(ctx, R, ra, rw, rb, psi->site(i), na, H, i, psi->site(i), nb, psi->d, out.c());
+        if (ctx->mixed)
+            mixed_env_right(ctx, R, ra, rw, rb, psi->site(i), na, H->Mr[i - 1].c(), psi->d, nw,
+                            psi->site(i), nb, out.c());
+        else
+            env_right(ctx, R, ra, rw, rb, psi->site(i), na, H, i, psi->site(i), nb, psi->d, out.c());
         blk[i] = std::move(out);
         a[i] = na;
         w[i] = nw;
@@ -272,6 +280,14 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
     TN_REQUIRE(N >= 2, "DMRG needs at least two sites");
     TN_REQUIRE(o.precision == TN_PREC_FP64 || o.precision == TN_PREC_MIXED, "unknown precision");
     auto t0 = std::chrono::steady_clock::now();
+    // mixed precision: environment updates and truncation projections run on
+    // the tensor cores for the whole call; restored on every exit path
+    struct MixedMode {
+        Ctx* c;
+        bool old;
+        ~MixedMode() { c->mixed = old; }
+    } mode_guard{ctx, ctx->mixed};
+    ctx->mixed = (o.precision == TN_PREC_MIXED);
     movecenter(psi, 1, no_trunc());
     EnvCache env(psi, H);
     env.movecenter(1);
@@ -381,9 +397,12 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
     }
     double e64 = cost.x;
     if (o.precision == TN_PREC_MIXED && !sample_done) {
-        // FP64 recomputation of the energy at the final centre: <psi|H|psi>
-        env.movecenter(psi->center);
-        e64 = env.calculate().x;
+        // FP64 recomputation of the energy: <psi|H|psi> from environments
+        // rebuilt in FP64 (the sweep's own blocks carry 3xTF32 rounding)
+        ctx->mixed = false;
+        EnvCache env64(psi, H);
+        env64.movecenter(psi->center);
+        e64 = env64.calculate().x;
     }
     *energy = cost.x;
     if (stats) {

@@ -20,7 +20,8 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
                                                     const cplx* __restrict__ A, int64_t lda,
                                                     int64_t sA, const cplx* __restrict__ B,
                                                     int64_t ldb, int64_t sB, cplx beta,
-                                                    cplx* __restrict__ C, int64_t ldc, int64_t sC) {
+                                                    cplx* __restrict__ C, int64_t ldc, int64_t sC,
+                                                    int lower) {
     __shared__ cplx As[GB_K][GB_M + 1];
     __shared__ cplx Bs[GB_K][GB_N + 1];
     const int tid = threadIdx.x;
@@ -30,6 +31,9 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
     B += bz * sB;
     C += bz * sC;
     const int64_t m0 = (int64_t)blockIdx.x * GB_M, n0 = (int64_t)blockIdx.y * GB_N;
+    // lower: only the lower triangle is wanted (a Hermitian Gram matrix read
+    // by a LOWER-mode eigensolver); tiles strictly above the diagonal skip
+    if (lower && n0 >= m0 + GB_M) return;
     cplx acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -107,19 +111,19 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
 template <int OPA>
 void zgemm_dispatch_b(Ctx* ctx, Op opb, dim3 grid, int64_t m, int64_t n, int64_t k, cplx alpha,
                       const cplx* A, int64_t lda, int64_t sA, const cplx* B, int64_t ldb,
-                      int64_t sB, cplx beta, cplx* C, int64_t ldc, int64_t sC) {
+                      int64_t sB, cplx beta, cplx* C, int64_t ldc, int64_t sC, int lower) {
     switch (opb) {
         case OP_N:
-            zgemm_kernel<OPA, OP_N><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+            zgemm_kernel<OPA, OP_N><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
             break;
         case OP_T:
-            zgemm_kernel<OPA, OP_T><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+            zgemm_kernel<OPA, OP_T><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
             break;
         case OP_C:
-            zgemm_kernel<OPA, OP_C><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+            zgemm_kernel<OPA, OP_C><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
             break;
         case OP_R:
-            zgemm_kernel<OPA, OP_R><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+            zgemm_kernel<OPA, OP_R><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
             break;
     }
 }
@@ -439,20 +443,21 @@ inline int grid_for(Ctx* ctx, int64_t n, int threads = 256) {
 // -------------------------------------------------------------------------
 void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha, const cplx* A,
            int64_t lda, int64_t sA, const cplx* B, int64_t ldb, int64_t sB, cplx beta, cplx* C,
-           int64_t ldc, int64_t sC, int64_t batch) {
+           int64_t ldc, int64_t sC, int64_t batch, bool lower_only) {
     if (m <= 0 || n <= 0 || batch <= 0) return;
+    const int lower = lower_only ? 1 : 0;
     TN_REQUIRE((n + GB_N - 1) / GB_N <= 65535 && batch <= 65535, "zgemm: grid too large");
     dim3 grid((unsigned)((m + GB_M - 1) / GB_M), (unsigned)((n + GB_N - 1) / GB_N), (unsigned)batch);
     if (k <= 0) {  // C = beta * C
         alpha = cmk(0, 0);
     }
-    ProfScope ps(ctx, 1, 8.0 * m * n * (double)std::max<int64_t>(k, 0) * batch,
+    ProfScope ps(ctx, 1, (lower ? 0.5 : 1.0) * 8.0 * m * n * (double)std::max<int64_t>(k, 0) * batch,
                  16.0 * (double)(m * k + k * n + m * n) * batch);
     switch (opa) {
-        case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
-        case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
-        case OP_C: zgemm_dispatch_b<OP_C>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
-        case OP_R: zgemm_dispatch_b<OP_R>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC); break;
+        case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
+        case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
+        case OP_C: zgemm_dispatch_b<OP_C>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
+        case OP_R: zgemm_dispatch_b<OP_R>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
     }
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());

@@ -8,6 +8,7 @@
 // needed.  The Gram product runs on our GEMM, the Hermitian eigenproblem on
 // cuSOLVER's zheevd (FP64), and the keep rule on the warp-shuffle kernel.
 #include "common.cuh"
+#include "mixed.cuh"
 
 #include <cstring>
 
@@ -158,9 +159,9 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
     double* dS = lam + g;
     const cplx one = cmk(1, 0), zero = cmk(0, 0);
     if (left_iso)  // G = theta theta^H
-        zgemm(ctx, OP_N, OP_C, m, m, n, one, theta, m, 0, theta, m, 0, zero, G, m, 0);
+        zgemm(ctx, OP_N, OP_C, m, m, n, one, theta, m, 0, theta, m, 0, zero, G, m, 0, 1, true);
     else  // G = theta^H theta
-        zgemm(ctx, OP_C, OP_N, n, n, m, one, theta, m, 0, theta, m, 0, zero, G, n, 0);
+        zgemm(ctx, OP_C, OP_N, n, n, m, one, theta, m, 0, theta, m, 0, zero, G, n, 0, 1, true);
     heevd(ctx, G, g, lam);
     KeepResult kr = keep_rule(ctx, lam, g, sz, cutoff, maxdim, mindim, dS);
     const int64_t k = kr.k;
@@ -168,13 +169,19 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
         take_top_eigvecs(ctx, G, m, k, X.c());
-        zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
+        if (ctx->mixed)  // the isometry stays exact; the projection on the tensor cores
+            mixed_gemm(ctx, k, n, m, X.c(), true, theta, Y.c());
+        else
+            zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
     } else {
         DBuf V(ctx, sizeof(cplx) * n * k);
         take_top_eigvecs(ctx, G, n, k, V.c());
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
-        zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V.c(), n, 0, zero, X.c(), m, 0);
+        if (ctx->mixed)
+            mixed_gemm(ctx, m, k, n, theta, false, V.c(), X.c());
+        else
+            zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V.c(), n, 0, zero, X.c(), m, 0);
         conj_transpose(ctx, V.c(), n, k, Y.c());  // Y = V^H (k x n)
     }
     if (S) {

@@ -145,6 +145,123 @@ __global__ void __launch_bounds__(256) heff_mid_kernel(
     }
 }
 
+// ---- environment legs ------------------------------------------------------
+constexpr int ENV_MAX = 16;  // w * d on either side of an MPO leg
+
+__device__ __forceinline__ void store_split(float* planes, size_t plane, size_t off, float re,
+                                            float im) {
+    const float rh = to_tf32(re), ih = to_tf32(im);
+    planes[off] = rh;
+    planes[plane + off] = ih;
+    planes[2 * plane + off] = to_tf32(re - rh);
+    planes[3 * plane + off] = to_tf32(im - ih);
+}
+
+// Left environment leg: X[(a w),(s b')] (K-chunk partials, FP32 planar,
+// column-major) -> Y[(a s'),(w' b')] = sum_{w,s} X Ml[(w,s),(s',w')], written
+// as split planes with rows (w' b') and K = (a s') (coalesced along a).
+__global__ void __launch_bounds__(128) env_left_leg_kernel(
+    const float* __restrict__ P, int S, int64_t chunk, int64_t M, int64_t plane_in, int64_t ca,
+    int wl, int d, int wr, const cplx* __restrict__ Ml, float* __restrict__ planes, int64_t ld,
+    int64_t rows) {
+    const int nI = wl * d, nJ = d * wr;
+    __shared__ float2 sM[ENV_MAX * ENV_MAX];
+    for (int t = threadIdx.x; t < nI * nJ; t += blockDim.x)
+        sM[t] = make_float2((float)Ml[t].x, (float)Ml[t].y);
+    __syncthreads();
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, bp = blockIdx.y;
+    if (a >= ca) return;
+    float2 x[ENV_MAX];
+#pragma unroll
+    for (int I = 0; I < ENV_MAX; ++I) {
+        x[I] = make_float2(0.f, 0.f);
+        if (I < nI) {
+            const int w = I % wl, s = I / wl;
+            const int64_t off = (a + ca * w) + M * (s + (int64_t)d * bp);
+            double sr = 0.0, si = 0.0;
+            for (int z = 0; z < S; ++z) {
+                sr += (double)P[(size_t)z * chunk + off];
+                si += (double)P[(size_t)z * chunk + plane_in + off];
+            }
+            x[I] = make_float2((float)sr, (float)si);
+        }
+    }
+    const size_t plane = (size_t)rows * ld;
+    for (int J = 0; J < nJ; ++J) {
+        float yr = 0.f, yi = 0.f;
+#pragma unroll
+        for (int I = 0; I < ENV_MAX; ++I) {
+            if (I < nI) {
+                const float2 m = sM[I + nI * J];
+                yr = fmaf(x[I].x, m.x, fmaf(-x[I].y, m.y, yr));
+                yi = fmaf(x[I].x, m.y, fmaf(x[I].y, m.x, yi));
+            }
+        }
+        const int sp = J % d, wp = J / d;
+        const int64_t n = wp + (int64_t)wr * bp, k = a + ca * sp;
+        store_split(planes, plane, (size_t)n * ld + k, yr, yi);
+    }
+}
+
+// Right environment leg: Z[(a s'),(w' b')] partials -> Z2[(a w),(s b')] =
+// sum_{s',w'} Z Mr[(s',w'),(w,s)], written as split planes with rows (a w)
+// and K = (s b'), staged through shared memory (32 a x 8 b' per block).
+constexpr int ENVR_A = 32, ENVR_B = 8;
+__global__ void __launch_bounds__(256) env_right_leg_kernel(
+    const float* __restrict__ P, int S, int64_t chunk, int64_t M, int64_t plane_in, int64_t ca,
+    int64_t cb2, int wl, int d, int wr, const cplx* __restrict__ Mr, float* __restrict__ planes,
+    int64_t ld, int64_t rows) {
+    const int nI = d * wr, nJ = wl * d;
+    __shared__ float2 sM[ENV_MAX * ENV_MAX];
+    __shared__ float2 sY[ENVR_B][ENVR_A][ENV_MAX];
+    for (int t = threadIdx.x; t < nI * nJ; t += blockDim.x)
+        sM[t] = make_float2((float)Mr[t].x, (float)Mr[t].y);
+    __syncthreads();
+    const int ta = threadIdx.x & 31, tb = threadIdx.x >> 5;
+    const int64_t a = (int64_t)blockIdx.x * ENVR_A + ta, bp = (int64_t)blockIdx.y * ENVR_B + tb;
+    float2 x[ENV_MAX];
+#pragma unroll
+    for (int I = 0; I < ENV_MAX; ++I) {
+        x[I] = make_float2(0.f, 0.f);
+        if (I < nI && a < ca && bp < cb2) {
+            const int sp = I % d, wp = I / d;
+            const int64_t off = (a + ca * sp) + M * (wp + (int64_t)wr * bp);
+            double sr = 0.0, si = 0.0;
+            for (int z = 0; z < S; ++z) {
+                sr += (double)P[(size_t)z * chunk + off];
+                si += (double)P[(size_t)z * chunk + plane_in + off];
+            }
+            x[I] = make_float2((float)sr, (float)si);
+        }
+    }
+    for (int J = 0; J < nJ; ++J) {
+        float yr = 0.f, yi = 0.f;
+#pragma unroll
+        for (int I = 0; I < ENV_MAX; ++I) {
+            if (I < nI) {
+                const float2 m = sM[I + nI * J];
+                yr = fmaf(x[I].x, m.x, fmaf(-x[I].y, m.y, yr));
+                yi = fmaf(x[I].x, m.y, fmaf(x[I].y, m.x, yi));
+            }
+        }
+        sY[tb][ta][J] = make_float2(yr, yi);
+    }
+    __syncthreads();
+    // rows (a + ca*w) of this block's a range; columns k = s + d*b' of its b' range
+    const size_t plane = (size_t)rows * ld;
+    const int ncol = d * ENVR_B, nrow = ENVR_A * wl;
+    for (int e = threadIdx.x; e < nrow * ncol; e += blockDim.x) {
+        const int col = e % ncol, row = e / ncol;
+        const int al = row % ENVR_A, w = row / ENVR_A;
+        const int s = col % d, bl = col / d;
+        const int64_t ag = (int64_t)blockIdx.x * ENVR_A + al;
+        const int64_t bg = (int64_t)blockIdx.y * ENVR_B + bl;
+        if (ag >= ca || bg >= cb2) continue;
+        const float2 v = sY[bl][al][w + wl * s];
+        store_split(planes, plane, (size_t)(ag + ca * w) * ld + (s + (int64_t)d * bg), v.x, v.y);
+    }
+}
+
 // zero the K padding columns [K, ld) of T2 planes (only when ld > K)
 __global__ void zero_pad_kernel(float* planes, int64_t rows, int64_t K, int64_t ld) {
     const int64_t pad = ld - K;
@@ -252,6 +369,86 @@ void mixed_heff2(Ctx* ctx, MixedWork& mw, const cplx* W12, int64_t cl, int64_t c
     TN_REQUIRE(mw.cl == cl && mw.cr == cr && mw.wl == wl && mw.wr == wr && mw.d == d,
                "mixed H_eff: environment not prepared for this bond");
     heff2_planes(ctx, mw, W12, cl, cr, d, wl, wr, x, y);
+}
+
+// L'[a',w',b'] = sum L[a,w,b] conj(A[a,s',a']) W[w,s',s,w'] B[b,s,b']
+// (projmps.jl:50-66) with both GEMMs on the tensor cores.
+void mixed_env_left(Ctx* ctx, const cplx* L, int64_t ca, int64_t wl, int64_t cb, const cplx* A,
+                    int64_t ca2, const cplx* Ml, int d, int64_t wr, const cplx* B, int64_t cb2,
+                    cplx* out) {
+    TN_REQUIRE(wl * d <= ENV_MAX && wr * d <= ENV_MAX, "mixed environment: MPO bond too large");
+    TcPlanes pL, pB, pY, pA;
+    // X[(a w), (s b')] = L[(a w), b] B[b, (s b')]
+    split_transpose(ctx, L, ca * wl, cb, ca * wl, pL, ctx->s_mixa);
+    split_natural(ctx, B, d * cb2, cb, pB, ctx->s_mixb);
+    const int64_t M1 = ca * wl, N1 = d * cb2;
+    const int S1 = tc_chunks(cb);
+    const int64_t ch1 = 2 * M1 * N1;
+    float* P1 = static_cast<float*>(ctx->s_mixc.get(ctx, sizeof(float) * (size_t)S1 * ch1));
+    tc_cgemm_partials(ctx, pL, pB, M1, N1, cb, false, TC_KCHUNK, P1, M1, M1 * N1, ch1);
+    // Y as split planes, rows (w' b'), K = (a s')
+    pY.rows = wr * cb2;
+    pY.K = ca * d;
+    pY.ld = tc_ld(pY.K);
+    pY.p = static_cast<float*>(ctx->s_mixd.get(ctx, sizeof(float) * pY.floats()));
+    {
+        ProfScope ps(ctx, 4, 8.0 * ca * cb2 * (wl * d) * (d * wr),
+                     8.0 * (double)S1 * M1 * N1 + 16.0 * (double)pY.rows * pY.K);
+        dim3 grid((unsigned)((ca + 127) / 128), (unsigned)cb2);
+        env_left_leg_kernel<<<grid, 128, 0, ctx->stream>>>(P1, S1, ch1, M1, M1 * N1, ca, (int)wl, d,
+                                                           (int)wr, Ml, pY.p, pY.ld, pY.rows);
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+    }
+    // out[a', (w' b')] = conj(A)[(a s'), a']^T Y
+    split_natural(ctx, A, ca2, ca * d, pA, ctx->s_mixa);
+    const int64_t M3 = ca2, N3 = wr * cb2;
+    const int S3 = tc_chunks(ca * d);
+    const int64_t ch3 = 2 * M3 * N3;
+    float* P3 = static_cast<float*>(ctx->s_mixe.get(ctx, sizeof(float) * (size_t)S3 * ch3));
+    tc_cgemm_partials(ctx, pA, pY, M3, N3, ca * d, true, TC_KCHUNK, P3, M3, M3 * N3, ch3);
+    tc_reduce_fp64(ctx, P3, S3, M3, N3, M3, M3 * N3, ch3, out, M3, false);
+}
+
+// R[a,w,b] = sum B[b,s,b'] R'[a',w',b'] W[w,s',s,w'] conj(A[a,s',a'])
+// (projmps.jl:74-95) with both GEMMs on the tensor cores.
+void mixed_env_right(Ctx* ctx, const cplx* R, int64_t ca2, int64_t wr, int64_t cb2, const cplx* A,
+                     int64_t ca, const cplx* Mr, int d, int64_t wl, const cplx* B, int64_t cb,
+                     cplx* out) {
+    TN_REQUIRE(wl * d <= ENV_MAX && wr * d <= ENV_MAX, "mixed environment: MPO bond too large");
+    TcPlanes pA, pR, pZ, pB;
+    // Z[(a s'), (w' b')] = conj(A)[(a s'), a'] R[a', (w' b')]
+    split_transpose(ctx, A, ca * d, ca2, ca * d, pA, ctx->s_mixa);
+    split_natural(ctx, R, wr * cb2, ca2, pR, ctx->s_mixb);
+    const int64_t M1 = ca * d, N1 = wr * cb2;
+    const int S1 = tc_chunks(ca2);
+    const int64_t ch1 = 2 * M1 * N1;
+    float* P1 = static_cast<float*>(ctx->s_mixc.get(ctx, sizeof(float) * (size_t)S1 * ch1));
+    tc_cgemm_partials(ctx, pA, pR, M1, N1, ca2, true, TC_KCHUNK, P1, M1, M1 * N1, ch1);
+    // Z2 as split planes, rows (a w), K = (s b')
+    pZ.rows = ca * wl;
+    pZ.K = d * cb2;
+    pZ.ld = tc_ld(pZ.K);
+    pZ.p = static_cast<float*>(ctx->s_mixd.get(ctx, sizeof(float) * pZ.floats()));
+    {
+        ProfScope ps(ctx, 4, 8.0 * ca * cb2 * (wl * d) * (d * wr),
+                     8.0 * (double)S1 * M1 * N1 + 16.0 * (double)pZ.rows * pZ.K);
+        dim3 grid((unsigned)((ca + ENVR_A - 1) / ENVR_A), (unsigned)((cb2 + ENVR_B - 1) / ENVR_B));
+        TN_REQUIRE(grid.y <= 65535, "mixed environment: chi too large");
+        env_right_leg_kernel<<<grid, 256, 0, ctx->stream>>>(P1, S1, ch1, M1, M1 * N1, ca, cb2,
+                                                            (int)wl, d, (int)wr, Mr, pZ.p, pZ.ld,
+                                                            pZ.rows);
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+    }
+    // out[(a w), b] = Z2[(a w), (s b')] B[b, (s b')]^T
+    split_transpose(ctx, B, cb, d * cb2, cb, pB, ctx->s_mixa);
+    const int64_t M3 = ca * wl, N3 = cb;
+    const int S3 = tc_chunks(d * cb2);
+    const int64_t ch3 = 2 * M3 * N3;
+    float* P3 = static_cast<float*>(ctx->s_mixe.get(ctx, sizeof(float) * (size_t)S3 * ch3));
+    tc_cgemm_partials(ctx, pZ, pB, M3, N3, d * cb2, false, TC_KCHUNK, P3, M3, M3 * N3, ch3);
+    tc_reduce_fp64(ctx, P3, S3, M3, N3, M3, M3 * N3, ch3, out, M3, false);
 }
 
 // C (m x n, FP64 column-major) = op(A) B on the tensor cores.  A is m x k

@@ -92,3 +92,18 @@ def test_dmrg_mixed_matches_fp64(tn):
     _, Emx = tn.dmrg(pmx, W, precision="mixed", stats=st, **kw)
     assert abs(st["energy_fp64"] - E64) <= 1e-8 * abs(E64), (st["energy_fp64"], E64, Emx)
     assert abs(Emx - E64) <= 1e-5 * abs(E64)
+
+
+@pytest.mark.parametrize("cl,cr,wl,wr", [(1, 2, 1, 5), (9, 17, 5, 5), (64, 96, 5, 5), (300, 256, 5, 3)])
+def test_env_updates_mixed(tn, cl, cr, wl, wr):
+    ctx = tn.context()
+    rng = np.random.default_rng(11 + cl)
+    d = 2
+    A, W = crand(rng, cl, d, cr), crand(rng, wl, d, d, wr)
+    L, R = crand(rng, cl, wl, cl), crand(rng, cr, wr, cr)
+    outl = np.zeros((cr, wr, cr), dtype=np.complex128, order="F")
+    outr = np.zeros((cl, wl, cl), dtype=np.complex128, order="F")
+    ctx.check(ctx.lib.tn_env_left(ctx.h, cl, cr, d, wl, wr, dp(L), dp(A), dp(W), dp(outl), 1))
+    ctx.check(ctx.lib.tn_env_right(ctx.h, cl, cr, d, wl, wr, dp(R), dp(A), dp(W), dp(outr), 1))
+    assert rel(outl, O.core.env_left(L, A, W, A)) < TOL
+    assert rel(outr, O.core.env_right(R, A, W, A)) < TOL
