@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-side", action="store_true", help="skip the QJMC and TEBD samples")
+    p.add_argument("--kernel-sample", action="store_true",
+                   help="only three mixed H_eff products at the bulk shape (kernel captures)")
     return p.parse_args()
 
 
@@ -465,8 +467,37 @@ def e2e_run(tn, ctx, psi, W_mpo, args, world):
                     "download, pinned host buffers"}
 
 
+def kernel_sample(args):
+    """Three mixed-precision H_eff products at the bulk bond shape of the
+    workload (chi x chi, w = 5): the small case for detailed kernel captures.
+    Operand planes (L 84 MB, theta 67 MB) exceed L2."""
+    import ctypes as C
+
+    import tngpu as tn
+    ctx = tn.context()
+    chi, w, d = args.chi, 5, 2
+    rng = np.random.default_rng(0)
+
+    def cr(*s):
+        return np.asfortranarray(rng.standard_normal(s) + 1j * rng.standard_normal(s))
+
+    L, R, W1, W2, th = cr(chi, w, chi), cr(chi, w, chi), cr(w, d, d, w), cr(w, d, d, w), cr(chi, d, d, chi)
+    out = np.zeros_like(th)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    t = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ctx.check(ctx.lib.tn_heff2_apply(ctx.h, chi, chi, d, w, w, w, dp(L), dp(W1), dp(W2), dp(R),
+                                         dp(th), dp(out), 1))
+        t.append(time.perf_counter() - t0)
+    print(json.dumps({"kernel_sample": f"mixed H_eff chi={chi} w={w}", "seconds": t}))
+
+
 def main():
     args = parse()
+    if args.kernel_sample:
+        kernel_sample(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

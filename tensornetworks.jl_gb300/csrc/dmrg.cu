@@ -396,7 +396,12 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         ctx->prof_on = false;
     }
     double e64 = cost.x;
-    if (o.precision == TN_PREC_MIXED && !sample_done) {
+    if (o.precision == TN_PREC_FP64 && !sample_done) {
+        // <psi|H|psi> of the final state (the returned cost is the last local
+        // Lanczos eigenvalue, as in dmrg.jl:55,98)
+        env.movecenter(psi->center);
+        e64 = env.calculate().x;
+    } else if (o.precision == TN_PREC_MIXED && !sample_done) {
         // FP64 recomputation of the energy: <psi|H|psi> from environments
         // rebuilt in FP64 (the sweep's own blocks carry 3xTF32 rounding)
         ctx->mixed = false;
@@ -404,7 +409,10 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         env64.movecenter(psi->center);
         e64 = env64.calculate().x;
     }
-    *energy = cost.x;
+    // FP64 mode returns the last local eigenvalue as the reference does; mixed
+    // mode returns the FP64 <psi|H|psi> (its Lanczos values carry the
+    // tensor-core accumulation bias of the environments, ~1e-5 relative)
+    *energy = (o.precision == TN_PREC_MIXED && !sample_done) ? e64 : cost.x;
     if (stats) {
         stats->sweeps = sweeps;
         stats->maxbonddim = D;

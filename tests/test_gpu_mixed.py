@@ -74,9 +74,9 @@ def _xxz(tn, N):
 
 
 def test_dmrg_mixed_matches_fp64(tn):
-    """Mixed-precision DMRG (3xTF32 matvecs, FP64 Lanczos/truncation) against
-    the plain FP64 run from the same state: |dE/E| on the FP64-recomputed
-    energy and identical kept bond dimensions."""
+    """Mixed-precision DMRG (3xTF32 matvecs, environments and projections;
+    FP64 Lanczos and truncation) against the plain FP64 run from the same
+    state: |dE/E| <= 1e-9 on the FP64-recomputed energy."""
     N, D = 24, 8
     rng = np.random.default_rng(3)
     shapes = [((1 if i == 0 else D), 2, (1 if i == N - 1 else D)) for i in range(N)]
@@ -86,12 +86,18 @@ def test_dmrg_mixed_matches_fp64(tn):
     W = tn.MPO(tn.spinhalf(), _xxz(tn, N))
     kw = dict(maxdim=128, cutoff=1e-12, minsweeps=8, maxsweeps=8, numconverges=np.inf, verbose=False)
     p64 = tn.GMPS.from_tensors(po.tensors, po.center)
-    _, E64 = tn.dmrg(p64, W, **kw)
+    st64 = {}
+    tn.dmrg(p64, W, stats=st64, **kw)
+    E64 = st64["energy_fp64"]  # FP64 <psi|H|psi> of the FP64 run's final state
     pmx = tn.GMPS.from_tensors(po.tensors, po.center)
     st = {}
     _, Emx = tn.dmrg(pmx, W, precision="mixed", stats=st, **kw)
-    assert abs(st["energy_fp64"] - E64) <= 1e-8 * abs(E64), (st["energy_fp64"], E64, Emx)
-    assert abs(Emx - E64) <= 1e-5 * abs(E64)
+    # spec bound: |dE/E| <= 1e-9 for the FP64-recomputed energy
+    assert abs(st["energy_fp64"] - E64) <= 1e-9 * abs(E64), (st["energy_fp64"], E64, Emx)
+    assert Emx == st["energy_fp64"]  # mixed mode returns the FP64 Rayleigh quotient
+    # kept bond dimensions may differ by a few where sigma^2 sits at the 1e-12
+    # cutoff: mixed products perturb the state at ~1e-7
+    assert max(pmx.bonddims()) == max(p64.bonddims())
 
 
 @pytest.mark.parametrize("cl,cr,wl,wr", [(1, 2, 1, 5), (9, 17, 5, 5), (64, 96, 5, 5), (300, 256, 5, 3)])
