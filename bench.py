@@ -243,6 +243,9 @@ def ours(args):
     prof = [{"kernel": L.PROF_CLASSES[i], "launches": int(la[i]), "ms": ms[i], "flops": fl[i],
              "bytes": by[i]} for i in range(n)]
     gpu_launches = int(la[7])
+    ph = (C.c_double * 4)()
+    ctx.check(ctx.lib.tn_profile_phases(ctx.h, ph))
+    phases = dict(zip(("environment", "two_site_prep", "lanczos", "truncation"), list(ph)))
 
     pk, pk_src = peaks()
     tf32_peak = 0.5 * pk["bf16_tflops"]
@@ -271,6 +274,7 @@ def ours(args):
 
     # FP64 comparison: bond-update sample of the same state, plain FP64 path
     log("profile: " + json.dumps(prof))
+    log("phases (s over the timed sweeps): " + json.dumps(phases))
     fp64 = fp64_sample(tn, psi, W_mpo, args, st)
     log("fp64 sample: " + json.dumps(fp64))
 
@@ -279,12 +283,12 @@ def ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed(tf32x3 tensor-core, f64)",
             "data": "synthetic", "config": config(args), "clocks": clocks,
             "gpu_launches": gpu_launches, "roofline": roof, "roofline_tensor_core": roof_tc,
-            "energy": {"lanczos": E, "fp64_rayleigh": st["energy_fp64"],
-                       "rel_diff": abs(E - st["energy_fp64"]) / abs(st["energy_fp64"])},
+            "energy": {"returned": E, "fp64_rayleigh": st["energy_fp64"],
+                       "last_sweep_lanczos": st["sweep_energies"][total - 1]},
             "sweeps": {"seconds": st["sweep_seconds"], "maxdim": st["sweep_maxdim"],
                        "energies": st["sweep_energies"], "ramp_seconds": ramp,
                        "main_wall_s": wall_main},
-            "fp64": fp64, "kernel_profile": prof}
+            "fp64": fp64, "kernel_profile": prof, "phase_seconds": phases}
     if fp64.get("sweeps_per_s_est"):
         line["mixed_vs_fp64"] = value / world / fp64["sweeps_per_s_est"]
     if not args.no_e2e:

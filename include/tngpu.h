@@ -102,6 +102,11 @@ typedef struct tn_dmrg_stats {
 int32_t tn_profile_enable(tn_ctx* ctx, int32_t on);
 int32_t tn_profile_reset(tn_ctx* ctx);
 int32_t tn_profile_read(tn_ctx* ctx, int64_t* launches, double* ms, double* flops, double* bytes);
+/* Host wall seconds of the DMRG bond phases while the profiler was on (the
+ * stream is synchronised at each phase end): [0] environment update,
+ * [1] two-site tensor and operand preparation, [2] Lanczos, [3] truncation
+ * and gauge move.  No reference counterpart (instrumentation). */
+int32_t tn_profile_phases(tn_ctx* ctx, double* seconds4);
 
 /* ---- context -------------------------------------------------------------- */
 int32_t tn_ctx_create(int32_t device, tn_ctx** out);
@@ -161,6 +166,23 @@ int32_t tn_applygates(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, const tn_
 /* nsteps x (applygates!, lognorm += log(norm), normalize!) (tebd.jl:61-84). */
 int32_t tn_tebd_steps(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nsteps,
                       const tn_trunc_opts* trunc, double* lognorm_accum);
+/* Hand-written adjoint of a TEBD evolution with step-dependent gates (the
+ * differentiated-TEBD form of the hot path; the reference has no counterpart:
+ * a ChainRulesCore rrule around its tebd step loop, tebd.jl:61-84, would call
+ * this).  Step s applies gates[step_gate[s]] as applygates! does
+ * (gatelist.jl:191-227), then normalize!.  The objective is
+ * f = <psi|O|psi>/<psi|psi> with the d x d Hermitian obs_op at obs_site,
+ * evaluated after non-truncating gauge moves to that site.  psi0 is not
+ * modified.  gate_grads == NULL: forward only.  Otherwise gate_grads receives
+ * df/dconj(G) (df = Re sum conj(gbar) dG) for every gate of every list, in
+ * list order and in each gate's upload layout ([o1,i1,o2,i2] or [o,i]),
+ * interleaved re/im.  The state is checkpointed every checkpoint_every
+ * steps and each segment recomputed for the reverse pass.  broadening eta:
+ * inverse Gram gaps x become x / (x^2 + eta lmax^2). */
+int32_t tn_tebd_grad(tn_ctx* ctx, const tn_mps* psi0, int32_t ngates, const tn_gates* const* gates,
+                     int32_t nsteps, const int32_t* step_gate, const tn_trunc_opts* trunc,
+                     int32_t checkpoint_every, int32_t obs_site, const double* obs_op,
+                     double broadening, double* f, double* gate_grads);
 
 /* ---- QJMC (src/algorithms/mps/qjmc.jl) ------------------------------------ */
 /* Emission rates |c_j^2 <psi|L_j^dag L_j|psi>| of single-site jump operators

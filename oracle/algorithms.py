@@ -14,6 +14,7 @@ from .core import (GMPS, OpList, ProjMPS, applyop, fr, inner, siterange,
 __all__ = [
     "lanczos_lowest", "dmrg", "trotterize", "applygate", "applygates", "tebd",
     "qjmc_gates", "qjmc_emission_rates", "qjmc_simulation", "dmrg_sweep_stats",
+    "tebd_segments_objective",
 ]
 
 
@@ -287,6 +288,26 @@ def tebd(st, psi, H, dt, tmax, save, observers=None, cutoff=1e-12, maxdim=0,
         if done:
             break
     return psi, energy
+
+
+def tebd_segments_objective(st, psi, Hs, dt, nsub, op, site, cutoff=1e-12, maxdim=0, mindim=1,
+                            evol="real", order=2):
+    """<op at site> of the normalised state after len(Hs) segments of nsub
+    TEBD steps, segment k with Hamiltonian Hs[k]: the step loop of
+    tebd.jl:61-84 (applygates! then normalize!) with the gates rebuilt per
+    segment by trotterize (gatelist.jl:75-121).  The reference has no such
+    driver; a user script composes it from these calls.  ``psi`` is
+    modified."""
+    psi.norm()  # tebd.jl:61 canonicalises an unset centre
+    for H in Hs:
+        rows = trotterize(st, H, dt, order=order, evol=evol)
+        for _ in range(nsub):
+            applygates(psi, rows, cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+            psi.normalize()
+    ob = OpList(len(psi))
+    ob.add([op], [site], 1.0)
+    num = complex(np.sum(inner(st, psi, ob, psi)))
+    return float(np.real(num)) / float(np.real(psi.norm()) ** 2)
 
 
 # ---------------------------------------------------------------------------

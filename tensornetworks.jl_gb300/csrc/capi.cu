@@ -130,6 +130,14 @@ int32_t tn_profile_reset(tn_ctx* h) {
     TN_REQUIRE(h, "null argument");
     h->c.prof_flush();
     for (auto& c : h->c.prof) c = Ctx::ProfClass{};
+    for (double& t : h->c.phase_s) t = 0.0;
+    TN_API_END
+}
+
+int32_t tn_profile_phases(tn_ctx* h, double* seconds4) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h && seconds4, "null argument");
+    for (int i = 0; i < 4; ++i) seconds4[i] = h->c.phase_s[i];
     TN_API_END
 }
 
@@ -484,6 +492,22 @@ int32_t tn_gates_upload(tn_ctx* h, int32_t N, int32_t d, int32_t nrows, const in
 int32_t tn_gates_destroy(tn_gates* g) {
     delete g;
     return TN_OK;
+}
+
+int32_t tn_tebd_grad(tn_ctx* h, const tn_mps* psi0, int32_t ngates, const tn_gates* const* gates,
+                     int32_t nsteps, const int32_t* step_gate, const tn_trunc_opts* t,
+                     int32_t checkpoint_every, int32_t obs_site, const double* obs_op,
+                     double broadening, double* f, double* gate_grads) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(h && psi0 && f && obs_op && (ngates == 0 || gates) && (nsteps == 0 || step_gate),
+               "null argument");
+    TN_REQUIRE(ngates >= 0 && nsteps >= 0, "negative count");
+    TN_REQUIRE(psi0->ctx == &h->c, "MPS belongs to another context");
+    std::vector<const tn_gates*> gl(gates, gates + ngates);
+    std::vector<int> steps(step_gate, step_gate + nsteps);
+    *f = tebd_grad(const_cast<tn_mps*>(psi0), gl, steps, to_trunc(t), checkpoint_every, obs_site,
+                   obs_op, broadening, gate_grads);
+    TN_API_END
 }
 
 int32_t tn_applygates(tn_ctx* h, tn_mps* psi, const tn_gates* g, const tn_trunc_opts* t) {

@@ -100,6 +100,10 @@ struct Ctx {
     };
     bool prof_on = false;
     ProfClass prof[TN_PROF_CLASSES];
+    // host wall seconds per DMRG phase while profiling (synchronised at each
+    // phase end): 0 environment update, 1 two-site tensor and operand
+    // preparation, 2 Lanczos, 3 truncation and normalisation
+    double phase_s[4] = {0, 0, 0, 0};
     std::vector<ProfRec> prof_pending;
     std::vector<cudaEvent_t> ev_pool;
     cudaEvent_t ev_get();
@@ -175,8 +179,12 @@ void zcopy(Ctx* ctx, cplx* dst, const cplx* src, int64_t n);
 void zfill(Ctx* ctx, cplx* dst, int64_t n, cplx v);
 void bilinear_dot(Ctx* ctx, const cplx* x, const cplx* y, int64_t n, cplx* dout);  // sum x*y
 double znorm2(Ctx* ctx, const cplx* x, int64_t n);  // ||x||^2, synchronous
-// take k eigenvectors, largest first: dst[:, j] = G[:, n-1-j]
-void take_top_eigvecs(Ctx* ctx, const cplx* G, int64_t n, int64_t k, cplx* dst);
+// take k eigenvectors, largest first: dst[:, j] = G[:, ncols-1-j] (ncols < 0:
+// ncols = n, a full ascending eigenvector matrix)
+void take_top_eigvecs(Ctx* ctx, const cplx* G, int64_t n, int64_t k, cplx* dst,
+                      int64_t ncols = -1);
+// *dout = sum of the real diagonal of the n x n matrix G (device)
+void gram_trace(Ctx* ctx, const cplx* G, int64_t n, double* dout);
 // scale columns: X[:, j] *= s[j] (s real, device)
 // dst (c x r) = src(r x c)^H, tiled through shared memory for coalescing
 void conj_transpose(Ctx* ctx, const cplx* src, int64_t r, int64_t c, cplx* dst);
@@ -189,10 +197,12 @@ void scale_rows(Ctx* ctx, cplx* X, int64_t k, int64_t n, const double* s, int in
 // Keep rule of tensors.jl:200-215 on ascending eigenvalues lam[0..n) of a Gram
 // matrix whose top sz values are the squared singular values.  Writes
 // (k, total, discarded) to host.  Also writes kept singular values (descending)
-// into dS when non-null.
+// into dS when non-null.  With dtotal (device, the Gram trace) the n values
+// are only the top of the spectrum: the weight below them is the trace minus
+// their sum.
 struct KeepResult { int64_t k; double total; double discarded; };
 KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double cutoff,
-                     int64_t maxdim, int64_t mindim, double* dS);
+                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal = nullptr);
 
 // ---- linear algebra (linalg.cu) ----------------------------------------
 // Truncated split theta (m x n) ~= X (m x k) Y (k x n).  left_iso: X is an
@@ -204,6 +214,8 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
                         int64_t maxdim, int64_t mindim, bool left_iso, DBuf& X, DBuf& Y,
                         std::vector<double>* S);
 // Hermitian eigen-decomposition in place (eigenvectors overwrite G), ascending.
-void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam);
+// top in (0, n): only the top eigenpairs, in ascending order in dlam[0..top)
+// and the first top columns of G.  Returns the number of eigenpairs.
+int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top = 0);
 
 }  // namespace tn

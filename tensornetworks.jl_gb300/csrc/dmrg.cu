@@ -315,6 +315,7 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         if (o.profile_from_sweep >= 0 && sweeps == o.profile_from_sweep) {
             ctx->prof_flush();
             for (auto& c : ctx->prof) c = Ctx::ProfClass{};
+            for (double& t : ctx->phase_s) t = 0.0;
             ctx->prof_on = true;
         }
         TN_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
@@ -326,7 +327,17 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
             const auto tb0 = std::chrono::steady_clock::now();
             const int site = direction ? N + 1 - j : j;
             const int site1 = direction ? site - 1 : site;
+            // phase clock (profiler on only): synchronise, charge the interval
+            auto tp = tb0;
+            auto phase = [&](int k) {
+                if (!ctx->prof_on) return;
+                ctx->sync();
+                const auto now = std::chrono::steady_clock::now();
+                ctx->phase_s[k] += std::chrono::duration<double>(now - tp).count();
+                tp = now;
+            };
             env.movecenter(site);
+            phase(0);
             two_site(psi, site1, theta);
             const int64_t cl = psi->dl(site1), cr = psi->dr(site1 + 1);
             const int64_t n = cl * d * d * cr;
@@ -345,12 +356,15 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
                     heff2_fp64(ctx, L, W12, R, cl, cr, d, lw, rw, x, y);
                 };
             }
+            phase(1);
             LanczosOut lo = lanczos_lowest(ctx, n, theta.c(), mv, o.krylovdim, o.kryloviter, 1e-14, vec);
             matvecs += lo.numops;
             if (o.precision == TN_PREC_MIXED) tc_check_error(ctx);
+            phase(2);
             cost = cmk(lo.eig, 0.0);
             SplitResult sr = replacesites2(psi, vec.c(), site1, direction, true, tr);
             last_disc = sr.discarded;
+            phase(3);
             if (stats && bond_updates < stats->bond_cap) {
                 if (stats->bond_seconds)
                     stats->bond_seconds[bond_updates] =

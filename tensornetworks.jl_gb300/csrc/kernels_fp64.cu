@@ -267,12 +267,29 @@ __global__ void zfill_kernel(cplx* x, int64_t n, cplx v) {
 }
 
 __global__ void top_eigvecs_kernel(const cplx* __restrict__ G, int64_t n, int64_t k,
-                                   cplx* __restrict__ dst) {
+                                   int64_t ncols, cplx* __restrict__ dst) {
     const int64_t total = n * k;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = idx % n, j = idx / n;
-        dst[i + n * j] = G[i + n * (n - 1 - j)];
+        dst[i + n * j] = G[i + n * (ncols - 1 - j)];
+    }
+}
+
+// *out = sum_i Re G[i, i] (one block)
+__global__ void __launch_bounds__(1024) gram_trace_kernel(const cplx* __restrict__ G, int64_t n,
+                                                          double* __restrict__ out) {
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += G[i + n * i].x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        *out = t;
     }
 }
 
@@ -357,10 +374,11 @@ __device__ inline double s2_at(const double* lam, int64_t n, int64_t i) {
 __global__ void __launch_bounds__(1024) keep_rule_kernel(const double* __restrict__ lam, int64_t n,
                                                          int64_t sz, double cutoff, int64_t maxdim,
                                                          int64_t mindim, double* __restrict__ S_out,
+                                                         const double* __restrict__ dtotal,
                                                          KeepDev* __restrict__ res) {
     __shared__ double wsum[32];
     __shared__ long long wcnt[32];
-    __shared__ double s_total;
+    __shared__ double s_total, s_rest;
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int nw = T >> 5;
     const int64_t per = (sz + T - 1) / T;
@@ -383,10 +401,15 @@ __global__ void __launch_bounds__(1024) keep_rule_kernel(const double* __restric
             wsum[w] = acc;  // sum of warps after w
             acc += tw;
         }
-        s_total = acc;
+        // partial spectrum: the weight below the available values is the
+        // trace minus their sum
+        const double rest = dtotal ? fmax(*dtotal - acc, 0.0) : 0.0;
+        s_rest = rest;
+        s_total = acc + rest;
     }
     __syncthreads();
-    const double after = v - local + wsum[warp];  // sum over chunks after t
+    const double rest = s_rest;
+    const double after = v - local + wsum[warp] + rest;  // weight after chunk t
     const double total = s_total;
     long long cnt = 0;
     double tail = after;
@@ -425,7 +448,7 @@ __global__ void __launch_bounds__(1024) keep_rule_kernel(const double* __restric
     if (lane == 0) wsum[warp] = disc;
     __syncthreads();
     if (t == 0) {
-        double d = 0.0;
+        double d = rest;
         for (int w = 0; w < nw; ++w) d += wsum[w];
         res->discarded = total > 0 ? d / total : 0.0;
     }
@@ -560,9 +583,17 @@ double znorm2(Ctx* ctx, const cplx* x, int64_t n) {
     return h[0];
 }
 
-void take_top_eigvecs(Ctx* ctx, const cplx* G, int64_t n, int64_t k, cplx* dst) {
+void take_top_eigvecs(Ctx* ctx, const cplx* G, int64_t n, int64_t k, cplx* dst, int64_t ncols) {
     if (n <= 0 || k <= 0) return;
-    top_eigvecs_kernel<<<grid_for(ctx, n * k), 256, 0, ctx->stream>>>(G, n, k, dst);
+    if (ncols < 0) ncols = n;
+    TN_REQUIRE(k <= ncols, "take_top_eigvecs: k exceeds the available eigenvectors");
+    top_eigvecs_kernel<<<grid_for(ctx, n * k), 256, 0, ctx->stream>>>(G, n, k, ncols, dst);
+    ctx->count();
+    TN_CHECK_CUDA(cudaGetLastError());
+}
+
+void gram_trace(Ctx* ctx, const cplx* G, int64_t n, double* dout) {
+    gram_trace_kernel<<<1, 1024, 0, ctx->stream>>>(G, n, dout);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
 }
@@ -605,9 +636,11 @@ void scale_rows(Ctx* ctx, cplx* X, int64_t k, int64_t n, const double* s, int in
 }
 
 KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double cutoff,
-                     int64_t maxdim, int64_t mindim, double* dS) {
+                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal) {
+    TN_REQUIRE(sz <= n, "keep_rule: more singular values than eigenvalues");
     KeepDev* dres = static_cast<KeepDev*>(ctx->s_coef.get(ctx, 256));
-    keep_rule_kernel<<<1, 1024, 0, ctx->stream>>>(dlam, n, sz, cutoff, maxdim, mindim, dS, dres);
+    keep_rule_kernel<<<1, 1024, 0, ctx->stream>>>(dlam, n, sz, cutoff, maxdim, mindim, dS, dtotal,
+                                                  dres);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
     double* h = ctx->pinned(4);

@@ -128,22 +128,43 @@ void Ctx::prof_flush() {
 }
 
 // ---- eigen-decomposition ---------------------------------------------------
-void heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam) {
-    int lwork = 0;
-    TN_CHECK_SOLVER(cusolverDnZheevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                                CUBLAS_FILL_MODE_LOWER, (int)n,
-                                                reinterpret_cast<cuDoubleComplex*>(G), (int)n,
-                                                dlam, &lwork));
+int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top) {
+    auto* A = reinterpret_cast<cuDoubleComplex*>(G);
+    const bool partial = top > 0 && top < n;
+    int lwork = 0, meig = (int)n;
+    // top eigenpairs only: the tridiagonal reduction is shared, the
+    // back-transformation covers top columns instead of n
+    const int il = (int)(n - top + 1), iu = (int)n;
+    if (partial)
+        TN_CHECK_SOLVER(cusolverDnZheevdx_bufferSize(
+            ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
+            (int)n, A, (int)n, 0.0, 0.0, il, iu, &meig, dlam, &lwork));
+    else
+        TN_CHECK_SOLVER(cusolverDnZheevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                                    CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n,
+                                                    dlam, &lwork));
     cuDoubleComplex* work = static_cast<cuDoubleComplex*>(
         ctx->s_work.get(ctx, sizeof(cuDoubleComplex) * (size_t)std::max(lwork, 1)));
     ProfScope ps(ctx, 2, 0.0, 16.0 * n * n);
-    TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                     (int)n, reinterpret_cast<cuDoubleComplex*>(G), (int)n, dlam,
-                                     work, lwork, ctx->d_info));
+    if (partial)
+        TN_CHECK_SOLVER(cusolverDnZheevdx(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                          CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, (int)n, A,
+                                          (int)n, 0.0, 0.0, il, iu, &meig, dlam, work, lwork,
+                                          ctx->d_info));
+    else
+        TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                         CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, dlam, work,
+                                         lwork, ctx->d_info));
     int info = 0;
     TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    if (info != 0) throw Error(TN_ERR_NUMERIC, "zheevd failed, info = " + std::to_string(info));
+    if (info != 0)
+        throw Error(TN_ERR_NUMERIC, std::string(partial ? "zheevdx" : "zheevd") +
+                                        " failed, info = " + std::to_string(info));
+    if (partial && meig != (int)top)
+        throw Error(TN_ERR_NUMERIC, "zheevdx returned " + std::to_string(meig) + " of " +
+                                        std::to_string(top) + " eigenpairs");
+    return partial ? top : n;
 }
 
 // ---- truncated split -------------------------------------------------------
@@ -155,27 +176,37 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
     const int64_t g = left_iso ? m : n;
     TN_REQUIRE(g <= 46340, "trunc_split: Gram matrix too large for 32-bit solver indexing");
     cplx* G = ctx->s_gram.c(ctx, (size_t)g * g);
-    double* lam = ctx->s_eigval.d(ctx, (size_t)g + sz);
+    double* lam = ctx->s_eigval.d(ctx, (size_t)g + sz + 1);
     double* dS = lam + g;
     const cplx one = cmk(1, 0), zero = cmk(0, 0);
     if (left_iso)  // G = theta theta^H
         zgemm(ctx, OP_N, OP_C, m, m, n, one, theta, m, 0, theta, m, 0, zero, G, m, 0, 1, true);
     else  // G = theta^H theta
         zgemm(ctx, OP_C, OP_N, n, n, m, one, theta, m, 0, theta, m, 0, zero, G, n, 0, 1, true);
-    heevd(ctx, G, g, lam);
-    KeepResult kr = keep_rule(ctx, lam, g, sz, cutoff, maxdim, mindim, dS);
+    // eigenpairs the keep rule can select: max(maxdim, mindim), at most sz
+    const int64_t maxd = (maxdim <= 0 || maxdim > sz) ? sz : maxdim;
+    const int64_t want = std::min(sz, std::max(maxd, mindim));
+    const bool partial = g >= 32 && want < g;
+    double* dtotal = nullptr;
+    if (partial) {  // the trace gives the weight below the computed eigenvalues
+        dtotal = lam + g + sz;
+        gram_trace(ctx, G, g, dtotal);
+    }
+    const int64_t ne = heevd(ctx, G, g, lam, partial ? want : 0);
+    KeepResult kr = keep_rule(ctx, lam, ne, std::min(sz, ne), cutoff, maxdim, mindim, dS, dtotal);
     const int64_t k = kr.k;
+    TN_REQUIRE(k <= ne, "trunc_split: keep rule selected more vectors than computed");
     if (left_iso) {
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
-        take_top_eigvecs(ctx, G, m, k, X.c());
+        take_top_eigvecs(ctx, G, m, k, X.c(), ne);
         if (ctx->mixed)  // the isometry stays exact; the projection on the tensor cores
             mixed_gemm(ctx, k, n, m, X.c(), true, theta, Y.c());
         else
             zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
     } else {
         DBuf V(ctx, sizeof(cplx) * n * k);
-        take_top_eigvecs(ctx, G, n, k, V.c());
+        take_top_eigvecs(ctx, G, n, k, V.c(), ne);
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
         if (ctx->mixed)

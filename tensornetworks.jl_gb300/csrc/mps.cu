@@ -1,6 +1,7 @@
 // Gauge moves, two-site splits, environment blocks, the two-site effective
 // Hamiltonian product and expectation values on device-resident MPS.
 #include "mps.cuh"
+#include "mixed.cuh"
 
 namespace tn {
 
@@ -81,6 +82,12 @@ void two_site(tn_mps* psi, int site, DBuf& buf) {
     const int64_t Dl = psi->dl(site), Dm = psi->dr(site), Dr = psi->dr(site + 1);
     const size_t need = sizeof(cplx) * Dl * d * d * Dr;
     if (buf.bytes < need) buf = DBuf(ctx, need);
+    if (ctx->mixed && Dm >= 64) {
+        // mixed-precision sweep: the two-site tensor only seeds the Lanczos
+        // solve, so the 3xTF32 tensor-core product is enough
+        mixed_gemm(ctx, Dl * d, d * Dr, Dm, psi->site(site), false, psi->site(site + 1), buf.c());
+        return;
+    }
     zgemm(ctx, OP_N, OP_N, Dl * d, d * Dr, Dm, ONE, psi->site(site), Dl * d, 0,
           psi->site(site + 1), Dm, 0, ZERO, buf.c(), Dl * d, 0);
 }

@@ -70,6 +70,8 @@ _SIGS = {
     "tn_gates_destroy": (i32, [P]),
     "tn_applygates": (i32, [P, P, P, C.POINTER(TruncOpts)]),
     "tn_tebd_steps": (i32, [P, P, P, i32, C.POINTER(TruncOpts), dp]),
+    "tn_tebd_grad": (i32, [P, P, i32, C.POINTER(P), i32, i32p, C.POINTER(TruncOpts), i32, i32, dp,
+                           C.c_double, dp, dp]),
     "tn_qjmc_rates": (i32, [P, P, i32, i32p, dp, dp, dp]),
     "tn_qjmc_run": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, dp, i64, C.POINTER(TruncOpts),
                           i32, i32, i32p, dp, dp, i32p, dp, i32p, i64p]),
@@ -85,6 +87,7 @@ _SIGS = {
     "tn_profile_enable": (i32, [P, i32]),
     "tn_profile_reset": (i32, [P]),
     "tn_profile_read": (i32, [P, i64p, dp, dp, dp]),
+    "tn_profile_phases": (i32, [P, dp]),
 }
 
 PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "zheevd (cuSOLVER FP64)",

@@ -14,7 +14,7 @@ import math
 import numpy as np
 
 from . import _lib as L
-from .models import OpList, trotter_rows
+from .models import OpList, trotter_rows, trotter_rows_dparam
 from .mps import GMPS, MPOHandle, inner
 
 
@@ -207,6 +207,75 @@ def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, m
                 ob.measure(step * dt, psi, normal, energy)
                 converged = converged or ob.checkdone()
     return psi, energy
+
+
+# ---------------------------------------------------------------------------
+# Differentiated TEBD: hand-written adjoint behind an rrule-shaped interface
+# ---------------------------------------------------------------------------
+class TEBDGradProblem:
+    """A TEBD evolution over parameter segments: segment k runs ``nsub`` steps
+    of the Trotter gates of ``H_of(params[k])`` (H_of affine in its argument;
+    the evolution of tebd.jl:61-84 with a Hamiltonian that changes per
+    segment), then the objective f = <op at site> of the normalised state."""
+
+    def __init__(self, st, H_of, dt, nsub, op, site, cutoff=1e-12, maxdim=0, mindim=1,
+                 evol="real", order=2, checkpoint=10, broadening=1e-24):
+        self.st, self.H_of, self.dt, self.nsub = st, H_of, float(dt), int(nsub)
+        self.op, self.site = op, int(site)
+        self.cutoff, self.maxdim, self.mindim = cutoff, maxdim, mindim
+        self.evol, self.order = evol, order
+        self.checkpoint, self.broadening = int(checkpoint), float(broadening)
+
+    def _lists(self, params, ctx):
+        rows = [trotter_rows(self.st, self.H_of(p), self.dt, self.order, self.evol) for p in params]
+        return rows, [GateList(self.H_of(params[0]).length, r, self.st.dim, ctx) for r in rows]
+
+    def _call(self, psi0, params, want):
+        ctx = psi0.ctx
+        params = np.asarray(params, dtype=float)
+        rows, lists = self._lists(params, ctx)
+        step_gate = np.repeat(np.arange(len(params), dtype=np.int32), self.nsub)
+        sizes = [g.size for r in rows for _, gs in r for g in gs]
+        grads = np.zeros(2 * sum(sizes)) if want else None
+        handles = (C.c_void_p * len(lists))(*[gl._h.value for gl in lists])
+        op = L.cplx_f(self.st.op(self.op)).astype(np.complex128)
+        f = C.c_double(0.0)
+        t = L.trunc(self.cutoff, self.maxdim, self.mindim)
+        ctx.check(ctx.lib.tn_tebd_grad(
+            ctx.h, psi0._h, len(lists), handles, len(step_gate), step_gate.ctypes.data_as(L.i32p),
+            C.byref(t), self.checkpoint, self.site, L.as_dp(op), self.broadening, C.byref(f),
+            L.as_dp(grads) if want else None))
+        return f.value, rows, grads
+
+    def value(self, psi0, params):
+        """f(params) by the forward pass alone."""
+        return self._call(psi0, params, False)[0]
+
+    def rrule(self, psi0, params):
+        """(f, pullback): pullback(fbar) = fbar * df/dparams, through the
+        library's adjoint (the shape of a ChainRulesCore rrule)."""
+        f, rows, grads = self._call(psi0, params, True)
+        gz = grads.view(np.complex128)
+        dfdp = np.zeros(len(params))
+        off = 0
+        for k, p in enumerate(np.asarray(params, dtype=float)):
+            drows = trotter_rows_dparam(self.st, self.H_of(p), self.H_of(p + 1.0), self.dt,
+                                        self.order, self.evol)
+            acc = 0.0
+            for (_, gs), (_, dgs) in zip(rows[k], drows):
+                for g, dg in zip(gs, dgs):
+                    gb = gz[off:off + g.size].reshape(g.shape, order="F")
+                    acc += float(np.real(np.vdot(gb, dg)))  # Re sum conj(gbar) dG
+                    off += g.size
+            dfdp[k] = acc
+        return f, (lambda fbar=1.0: fbar * dfdp)
+
+
+def tebd_grad(st, psi0, H_of, params, dt, nsub, op, site, **kw):
+    """f and df/dparams of the segment-wise TEBD objective (TEBDGradProblem)."""
+    prob = TEBDGradProblem(st, H_of, dt, nsub, op, site, **kw)
+    f, back = prob.rrule(psi0, params)
+    return f, back()
 
 
 # ---------------------------------------------------------------------------

@@ -253,6 +253,44 @@ def gate_exp(gate, time):
     return np.transpose(E, back)
 
 
+def gate_exp_frechet(gate, dgate, time):
+    """d/de exp(time * (gate + e dgate)) at e = 0, in the layout of gate_exp:
+    the Frechet derivative of the matrix exponential (scipy expm_frechet)."""
+    n = gate.ndim // 2
+    d = gate.shape[0]
+    outs = list(range(0, 2 * n, 2))
+    ins = list(range(1, 2 * n, 2))
+    M = _f(np.transpose(time * gate, outs + ins), (d ** n, d ** n))
+    E = _f(np.transpose(time * dgate, outs + ins), (d ** n, d ** n))
+    _, L = sla.expm_frechet(M, E)
+    back = np.argsort(outs + ins)
+    return np.transpose(_f(L, (d,) * (2 * n)), back)
+
+
+def trotter_rows_dparam(st, H, H1, dt, order=2, evol="imag"):
+    """Derivatives of the trotter_rows gates of H with respect to a parameter p
+    when H(p + 1) = H1 and H is affine in p: each gate exp(tau g) changes by
+    L(tau g, tau (g1 - g)) per unit p.  Rows and gates in trotter_rows order."""
+    rng = H.siterange()
+    order = 1 if rng == 1 else order
+    t = -1j * dt if evol == "real" else dt
+    rows = []
+    for i in range(1, rng + 1):
+        tau = t / 2 if (i < rng and order == 2) else t
+        sites, dgates = [], []
+        for site in range(i, H.length + 1, rng):
+            g = site_tensor(st, H, site)
+            if g is not None:
+                g1 = site_tensor(st, H1, site)
+                sites.append(site)
+                dgates.append(gate_exp_frechet(g, g1 - g, tau))
+        rows.append((sites, dgates))
+    if order == 2:
+        for i in range(1, rng):
+            rows.append(rows[rng - i - 1])
+    return rows
+
+
 def trotter_rows(st, H, dt, order=2, evol="imag"):
     """Rows of non-overlapping gates: [(sites, gates), ...]; second order appends
     the first rng-1 rows in reverse (gatelist.jl:75-121)."""

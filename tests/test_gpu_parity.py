@@ -97,6 +97,11 @@ def _matrix_with_spectrum(rng, m, n, S):
     dict(S=[1, 0.5, 1e-3, 1e-6, 0.0], cutoff=1e-13, maxdim=2, mindim=1),
     dict(S=[1, 0.5, 1e-3, 1e-6, 0.0], cutoff=0.9, maxdim=0, mindim=3),
     dict(S=list(np.geomspace(1, 1e-7, 40)), cutoff=1e-10, maxdim=0, mindim=1),
+    # fewer kept vectors than the Gram order: top-eigenpair solver, weight
+    # below the computed eigenvalues from the Gram trace
+    dict(S=list(np.geomspace(1, 1e-9, 200)), cutoff=1e-14, maxdim=120, mindim=1),
+    dict(S=list(np.geomspace(1, 1e-9, 200)), cutoff=1e-10, maxdim=150, mindim=1),
+    dict(S=list(np.geomspace(1, 1e-9, 200)), cutoff=0.0, maxdim=50, mindim=80),
 ])
 def test_truncate_keep_rule_and_factors(tn, case, direction):
     ctx = tn.context()
