@@ -166,6 +166,11 @@ int32_t tn_applygates(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, const tn_
 /* nsteps x (applygates!, lognorm += log(norm), normalize!) (tebd.jl:61-84). */
 int32_t tn_tebd_steps(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nsteps,
                       const tn_trunc_opts* trunc, double* lognorm_accum);
+/* tn_tebd_steps with a precision mode: TN_PREC_MIXED runs the two-site
+ * contraction and the truncation projections as 3xTF32 tensor-core products
+ * (the Gram matrix, its eigensolver, norms and normalisation stay FP64). */
+int32_t tn_tebd_steps_prec(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nsteps,
+                           const tn_trunc_opts* trunc, int32_t precision, double* lognorm_accum);
 /* Hand-written adjoint of a TEBD evolution with step-dependent gates (the
  * differentiated-TEBD form of the hot path; the reference has no counterpart:
  * a ChainRulesCore rrule around its tebd step loop, tebd.jl:61-84, would call

@@ -528,6 +528,27 @@ int32_t tn_tebd_steps(tn_ctx* h, tn_mps* psi, const tn_gates* g, int32_t nsteps,
     TN_API_END
 }
 
+int32_t tn_tebd_steps_prec(tn_ctx* h, tn_mps* psi, const tn_gates* g, int32_t nsteps,
+                           const tn_trunc_opts* t, int32_t precision, double* lognorm) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(psi && g, "null argument");
+    TN_REQUIRE(nsteps >= 0, "negative step count");
+    TN_REQUIRE(precision == TN_PREC_FP64 || precision == TN_PREC_MIXED, "unknown precision");
+    Ctx* ctx = psi->ctx;
+    // mixed: the two-site contraction and the truncation projections run on
+    // the tensor cores; the Gram matrix, eigensolver and norms stay FP64
+    struct Guard {
+        Ctx* c;
+        bool old;
+        ~Guard() { c->mixed = old; }
+    } guard{ctx, ctx->mixed};
+    ctx->mixed = precision == TN_PREC_MIXED;
+    tebd_steps(psi, g, nsteps, to_trunc(t), lognorm);
+    if (ctx->mixed) tc_check_error(ctx);
+    ctx->sync();
+    TN_API_END
+}
+
 int32_t tn_qjmc_rates(tn_ctx* h, tn_mps* psi, int32_t njump, const int32_t* sites,
                       const double* ops, const double* coeffs, double* rates) {
     TN_API_BEGIN(h ? &h->c : nullptr)

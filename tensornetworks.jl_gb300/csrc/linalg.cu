@@ -196,11 +196,14 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
     KeepResult kr = keep_rule(ctx, lam, ne, std::min(sz, ne), cutoff, maxdim, mindim, dS, dtotal);
     const int64_t k = kr.k;
     TN_REQUIRE(k <= ne, "trunc_split: keep rule selected more vectors than computed");
+    // tensor-core projection in mixed mode, for products large enough to pay
+    // for the operand conversion
+    const bool use_tc = ctx->mixed && (double)m * n * k >= (double)(1 << 21);
     if (left_iso) {
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
         take_top_eigvecs(ctx, G, m, k, X.c(), ne);
-        if (ctx->mixed)  // the isometry stays exact; the projection on the tensor cores
+        if (use_tc)  // the isometry stays exact; the projection on the tensor cores
             mixed_gemm(ctx, k, n, m, X.c(), true, theta, Y.c());
         else
             zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
@@ -209,7 +212,7 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
         take_top_eigvecs(ctx, G, n, k, V.c(), ne);
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
-        if (ctx->mixed)
+        if (use_tc)
             mixed_gemm(ctx, m, k, n, theta, false, V.c(), X.c());
         else
             zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V.c(), n, 0, zero, X.c(), m, 0);

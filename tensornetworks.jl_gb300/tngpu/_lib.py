@@ -70,6 +70,7 @@ _SIGS = {
     "tn_gates_destroy": (i32, [P]),
     "tn_applygates": (i32, [P, P, P, C.POINTER(TruncOpts)]),
     "tn_tebd_steps": (i32, [P, P, P, i32, C.POINTER(TruncOpts), dp]),
+    "tn_tebd_steps_prec": (i32, [P, P, P, i32, C.POINTER(TruncOpts), i32, dp]),
     "tn_tebd_grad": (i32, [P, P, i32, C.POINTER(P), i32, i32p, C.POINTER(TruncOpts), i32, i32, dp,
                            C.c_double, dp, dp]),
     "tn_qjmc_rates": (i32, [P, P, i32, i32p, dp, dp, dp]),

@@ -171,8 +171,10 @@ class TEBDOperators(TEBDObserver):
 
 
 def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, maxdim=0,
-         mindim=1, evol="imag", order=2, norm=0.0, verbose=False):
-    """Time evolution without projectors (tebd.jl:3-100); returns (psi, energy)."""
+         mindim=1, evol="imag", order=2, norm=0.0, verbose=False, precision="fp64"):
+    """Time evolution without projectors (tebd.jl:3-100); returns (psi, energy).
+    precision="mixed" runs the gate contractions and truncation projections
+    as 3xTF32 tensor-core products (FP64 Gram eigensolver and norms)."""
     if st.dim != psi.dim:
         raise ValueError("Sitetypes and MPS physical dimensions do not match.")
     if len(psi) != H.length:
@@ -195,7 +197,8 @@ def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, m
     converged = False
     while not converged:
         ln = C.c_double(0.0)
-        psi.ctx.check(psi.ctx.lib.tn_tebd_steps(psi.ctx.h, psi._h, gates._h, 1, C.byref(t), C.byref(ln)))
+        psi.ctx.check(psi.ctx.lib.tn_tebd_steps_prec(psi.ctx.h, psi._h, gates._h, 1, C.byref(t),
+                                                     L.PREC[precision], C.byref(ln)))
         normal += ln.value
         step += 1
         converged = step >= nsteps
@@ -219,7 +222,7 @@ class TEBDGradProblem:
     segment), then the objective f = <op at site> of the normalised state."""
 
     def __init__(self, st, H_of, dt, nsub, op, site, cutoff=1e-12, maxdim=0, mindim=1,
-                 evol="real", order=2, checkpoint=10, broadening=1e-24):
+                 evol="real", order=2, checkpoint=10, broadening=1e-32):
         self.st, self.H_of, self.dt, self.nsub = st, H_of, float(dt), int(nsub)
         self.op, self.site = op, int(site)
         self.cutoff, self.maxdim, self.mindim = cutoff, maxdim, mindim
