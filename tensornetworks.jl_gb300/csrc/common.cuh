@@ -201,8 +201,11 @@ void scale_rows(Ctx* ctx, cplx* X, int64_t k, int64_t n, const double* s, int in
 // are only the top of the spectrum: the weight below them is the trace minus
 // their sum.
 struct KeepResult { int64_t k; double total; double discarded; };
+// dinfo (device, optional): an eigensolver status read back in the same
+// synchronisation; nonzero raises TN_ERR_NUMERIC.
 KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double cutoff,
-                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal = nullptr);
+                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal = nullptr,
+                     const int* dinfo = nullptr);
 
 // ---- linear algebra (linalg.cu) ----------------------------------------
 // Truncated split theta (m x n) ~= X (m x k) Y (k x n).  left_iso: X is an
@@ -216,6 +219,7 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
 // Hermitian eigen-decomposition in place (eigenvectors overwrite G), ascending.
 // top in (0, n): only the top eigenpairs, in ascending order in dlam[0..top)
 // and the first top columns of G.  Returns the number of eigenpairs.
-int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top = 0);
+// check = false: the solver status stays in ctx->d_info for the caller.
+int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top = 0, bool check = true);
 
 }  // namespace tn

@@ -636,7 +636,8 @@ void scale_rows(Ctx* ctx, cplx* X, int64_t k, int64_t n, const double* s, int in
 }
 
 KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double cutoff,
-                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal) {
+                     int64_t maxdim, int64_t mindim, double* dS, const double* dtotal,
+                     const int* dinfo) {
     TN_REQUIRE(sz <= n, "keep_rule: more singular values than eigenvalues");
     KeepDev* dres = static_cast<KeepDev*>(ctx->s_coef.get(ctx, 256));
     keep_rule_kernel<<<1, 1024, 0, ctx->stream>>>(dlam, n, sz, cutoff, maxdim, mindim, dS, dtotal,
@@ -645,7 +646,13 @@ KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double
     TN_CHECK_CUDA(cudaGetLastError());
     double* h = ctx->pinned(4);
     TN_CHECK_CUDA(cudaMemcpyAsync(h, dres, sizeof(KeepDev), cudaMemcpyDeviceToHost, ctx->stream));
+    if (dinfo)
+        TN_CHECK_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(h + 3), dinfo, sizeof(int),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
+    if (dinfo && *reinterpret_cast<int*>(h + 3) != 0)
+        throw Error(TN_ERR_NUMERIC, "Hermitian eigensolver failed, info = " +
+                                        std::to_string(*reinterpret_cast<int*>(h + 3)));
     KeepDev r;
     memcpy(&r, h, sizeof(KeepDev));
     return KeepResult{r.k, r.total, r.discarded};

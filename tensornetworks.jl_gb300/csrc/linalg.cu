@@ -128,7 +128,7 @@ void Ctx::prof_flush() {
 }
 
 // ---- eigen-decomposition ---------------------------------------------------
-int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top) {
+int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top, bool check) {
     auto* A = reinterpret_cast<cuDoubleComplex*>(G);
     const bool partial = top > 0 && top < n;
     int lwork = 0, meig = (int)n;
@@ -155,12 +155,15 @@ int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top) {
         TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
                                          CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, dlam, work,
                                          lwork, ctx->d_info));
-    int info = 0;
-    TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->sync();
-    if (info != 0)
-        throw Error(TN_ERR_NUMERIC, std::string(partial ? "zheevdx" : "zheevd") +
-                                        " failed, info = " + std::to_string(info));
+    if (check) {
+        int info = 0;
+        TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        ctx->sync();
+        if (info != 0)
+            throw Error(TN_ERR_NUMERIC, std::string(partial ? "zheevdx" : "zheevd") +
+                                            " failed, info = " + std::to_string(info));
+    }
     if (partial && meig != (int)top)
         throw Error(TN_ERR_NUMERIC, "zheevdx returned " + std::to_string(meig) + " of " +
                                         std::to_string(top) + " eigenpairs");
@@ -192,8 +195,10 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
         dtotal = lam + g + sz;
         gram_trace(ctx, G, g, dtotal);
     }
-    const int64_t ne = heevd(ctx, G, g, lam, partial ? want : 0);
-    KeepResult kr = keep_rule(ctx, lam, ne, std::min(sz, ne), cutoff, maxdim, mindim, dS, dtotal);
+    // the solver status is read back with the keep-rule result (one synchronisation)
+    const int64_t ne = heevd(ctx, G, g, lam, partial ? want : 0, false);
+    KeepResult kr = keep_rule(ctx, lam, ne, std::min(sz, ne), cutoff, maxdim, mindim, dS, dtotal,
+                              ctx->d_info);
     const int64_t k = kr.k;
     TN_REQUIRE(k <= ne, "trunc_split: keep rule selected more vectors than computed");
     // tensor-core projection in mixed mode, for products large enough to pay

@@ -337,6 +337,52 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     return times, out, nj
 
 
+def shard_range(ntraj, rank, world):
+    """Contiguous block of trajectory indices [lo, hi) for one rank: the
+    first ntraj % world ranks take one extra trajectory."""
+    base, extra = divmod(int(ntraj), int(world))
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
+def qjmc_ensemble_sharded(st, psi, H, jumpops, tmax, dt, obs, ntraj, draws, group=None,
+                          run=None, **kw):
+    """qjmc_ensemble with the trajectories sharded over the ranks of a
+    torch.distributed process group (one process per GPU).  Each rank runs
+    its block of trajectories (draw rows lo:hi) with no data-path
+    collective; the trajectory-summed observables and the per-trajectory
+    jump counts are combined once at the end (all_reduce / all_gather on the
+    host).  Returns what qjmc_ensemble returns for all ntraj trajectories.
+    ``run`` replaces qjmc_ensemble (same signature), for host-only tests."""
+    import torch
+    import torch.distributed as dist
+    run = run or qjmc_ensemble
+    world = dist.get_world_size(group) if dist.is_initialized() else 1
+    rank = dist.get_rank(group) if dist.is_initialized() else 0
+    lo, hi = shard_range(ntraj, rank, world)
+    draws = np.asarray(draws)
+    if hi > lo:
+        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, hi - lo, draws=draws[lo:hi], **kw)
+        part = np.asarray(avg, dtype=np.complex128) * (hi - lo)
+    else:
+        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, 1, draws=draws[:1], **kw)
+        part = np.zeros_like(np.asarray(avg, dtype=np.complex128))
+        nj = np.zeros(0, dtype=np.int32)
+    if world == 1:
+        return times, part / ntraj, np.asarray(nj, dtype=np.int32)
+    buf = torch.from_numpy(np.ascontiguousarray(part.view(np.float64)))
+    dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    total = buf.numpy().view(np.complex128).reshape(part.shape)
+    # equal-size gather (padded to the largest block), trimmed per rank
+    m = -(-int(ntraj) // world)
+    mine = np.full(m, -1, dtype=np.int32)
+    mine[:hi - lo] = np.asarray(nj, dtype=np.int32)[:hi - lo]
+    counts = [torch.zeros(m, dtype=torch.int32) for _ in range(world)]
+    dist.all_gather(counts, torch.from_numpy(mine), group=group)
+    sizes = [shard_range(ntraj, r, world)[1] - shard_range(ntraj, r, world)[0] for r in range(world)]
+    return times, total / ntraj, np.concatenate([c.numpy()[:k] for c, k in zip(counts, sizes)])
+
+
 class QJMCOperators:
     """qjmc.jl:238-260"""
 
