@@ -54,8 +54,10 @@ def parse():
     p.add_argument("--no-side", action="store_true", help="skip the QJMC and TEBD samples")
     p.add_argument("--kernel-sample", action="store_true",
                    help="only three mixed H_eff products at the bulk shape (kernel captures)")
-    p.add_argument("--workload", default="dmrg", choices=["dmrg", "tebd-grad"],
-                   help="tebd-grad: the differentiated-TEBD gradient (own JSON line)")
+    p.add_argument("--workload", default="dmrg", choices=["dmrg", "tebd-grad", "tebd"],
+                   help="tebd-grad: the differentiated-TEBD gradient; tebd: the quench in FP64 "
+                        "and mixed precision (each its own JSON line)")
+    p.add_argument("--tebd-steps", type=int, default=60, help="tebd: steps of the quench")
     p.add_argument("--segments", type=int, default=100, help="tebd-grad: h segments")
     p.add_argument("--fd-coords", type=int, default=2,
                    help="tebd-grad: coordinates checked by central differences")
@@ -458,9 +460,12 @@ def e2e_run(tn, ctx, psi, W_mpo, args, world):
     h = C.c_void_p()
     ctx.check(ctx.lib.tn_mps_upload(ctx.h, len(ts), 2, dims, L.ptr_array(views), psi.center, C.byref(h)))
     g = tn.GMPS(h, len(ts), 2, ctx)
+    t_up = time.perf_counter() - t0
+    st = {}
     tn.dmrg(g, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=K, maxsweeps=K,
             numconverges=np.inf,
-            verbose=False, precision="mixed")
+            verbose=False, precision="mixed", stats=st)
+    t_dmrg = time.perf_counter() - t0 - t_up
     out = g.bonddims()
     outs = []
     for i in range(len(ts)):
@@ -472,8 +477,10 @@ def e2e_run(tn, ctx, psi, W_mpo, args, world):
     dbytes = sum(o.numel() * 8 for o in outs)
     return {"value": world * K / t, "unit": UNIT, "h2d_bytes_per_step": nbytes // K,
             "d2h_bytes_per_step": dbytes // K,
-            "note": "upload + tn_dmrg(K sweeps; re-canonicalises and rebuilds environments) + "
-                    "download, pinned host buffers"}
+            "breakdown_s": {"upload": t_up, "tn_dmrg": t_dmrg, "sweeps": float(sum(st["sweep_seconds"])),
+                            "download": t - t_up - t_dmrg},
+            "note": "upload + tn_dmrg(K sweeps; builds the environments, and at the end rebuilds "
+                    "them in FP64 for the returned energy) + download, pinned host buffers"}
 
 
 def kernel_sample(args):
@@ -570,8 +577,67 @@ def tebd_grad_run(args):
     print(json.dumps(line))
 
 
+def tebd_run(args):
+    """TEBD quench: N=64 XXZ (J=1, Delta=0.5) + 0.2(-1)^i Z_i, Neel start, real
+    time, 2nd order, dt=0.05, maxdim 256, cutoff 1e-10, <Z_i> and S(N/2) after
+    every step; the same run in FP64 and in mixed precision (3xTF32 gate
+    contractions and projections).  Reports steps/s of each and the largest
+    deviation of the mixed observables from FP64 over the run."""
+    import ctypes as C
+
+    import tngpu as tn
+    from tngpu import _lib as L
+    N, dt, steps = 64, 0.05, args.tebd_steps
+    H, Z = tn.OpList(N), tn.OpList(N)
+    for i in range(1, N):
+        H.add(["x", "x"], [i, i + 1], 1.0)
+        H.add(["y", "y"], [i, i + 1], 1.0)
+        H.add(["z", "z"], [i, i + 1], 0.5)
+    for i in range(1, N + 1):
+        H.add("z", i, 0.2 * (-1) ** i)
+        Z.add("z", i)
+    st = tn.spinhalf()
+    ctx = tn.context()
+    gates = tn.trotterize(st, H, dt, order=2, evol="real", ctx=ctx)
+    t = L.trunc(1e-10, 256, 1)
+    rec = {}
+    clk = Clocks(0)
+    for prec in ("fp64", "mixed"):
+        psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
+        psi.norm()
+        zs, ss, step_s = [], [], 0.0
+        ln = C.c_double(0.0)
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            ctx.check(ctx.lib.tn_tebd_steps_prec(ctx.h, psi._h, gates._h, 1, C.byref(t),
+                                                 L.PREC[prec], C.byref(ln)))
+            step_s += time.perf_counter() - t0
+            zs.append(np.real(tn.inner(st, psi, Z, psi)))
+            ss.append(psi.entropy(N // 2))
+        rec[prec] = {"steps_per_s": steps / step_s, "chi_end": psi.maxbonddim(),
+                     "z": np.asarray(zs), "s": np.asarray(ss)}
+        log(f"tebd {prec}: {steps / step_s:.3f} steps/s, chi_end {psi.maxbonddim()}")
+    clocks = clk.stop()
+    dz = float(np.max(np.abs(rec["mixed"]["z"] - rec["fp64"]["z"])))
+    ds = float(np.max(np.abs(rec["mixed"]["s"] - rec["fp64"]["s"])))
+    line = {"metric": "TEBD steps/s", "value": rec["fp64"]["steps_per_s"], "unit": "steps/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "c128 (f64)", "data": "synthetic",
+            "config": {"workload": f"N=64 XXZ J=1 Delta=0.5 + 0.2(-1)^i Z_i, Neel, dt=0.05, "
+                                   f"{steps} steps (t={steps * dt:.2f}), maxdim 256, cutoff 1e-10"},
+            "mixed_steps_per_s": rec["mixed"]["steps_per_s"],
+            "chi_end": {k: v["chi_end"] for k, v in rec.items()},
+            "mixed_vs_fp64_max_abs_dZ": dz, "mixed_vs_fp64_max_abs_dS": ds,
+            "fp64_final_S_half": float(rec["fp64"]["s"][-1]), "clocks": clocks,
+            "note": "steps/s counts the gate layers and the normalisation (tn_tebd_steps_prec); "
+                    "observables are measured between steps, outside the timing"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.workload == "tebd":
+        tebd_run(args)
+        return
     if args.workload == "tebd-grad":
         tebd_grad_run(args)
         return
