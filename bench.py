@@ -326,7 +326,7 @@ def ours(args):
         dist.destroy_process_group()
 
 
-def qjmc_sample(tn, ctx, pre_steps=100, steps=10, ntraj=256, workers=64):
+def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=256, workers=64):
     """BASELINE config 4 shapes: N=32 Ising chain H = sum Z Z + 0.8 sum X, jumps
     L_i = sqrt(0.1) s-_i, all-up start, dt=0.01, maxdim 64, cutoff 1e-10.  One
     trajectory is evolved `pre_steps` (untimed) so the timed steps run at grown

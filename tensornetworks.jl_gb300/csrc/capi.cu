@@ -505,7 +505,7 @@ int32_t tn_tebd_grad(tn_ctx* h, const tn_mps* psi0, int32_t ngates, const tn_gat
     TN_REQUIRE(psi0->ctx == &h->c, "MPS belongs to another context");
     std::vector<const tn_gates*> gl(gates, gates + ngates);
     std::vector<int> steps(step_gate, step_gate + nsteps);
-    *f = tebd_grad(const_cast<tn_mps*>(psi0), gl, steps, to_trunc(t), checkpoint_every, obs_site,
+    *f = tebd_grad(psi0, gl, steps, to_trunc(t), checkpoint_every, obs_site,
                    obs_op, broadening, gate_grads);
     TN_API_END
 }

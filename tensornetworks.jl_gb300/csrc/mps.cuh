@@ -95,7 +95,7 @@ std::vector<cplx> inner_terms(Ctx* ctx, const tn_mps* bra, const tn_mps* ket,
 // TEBD adjoint (tebd_grad.cu): f = <O at obs_site> after the steps (step s
 // applies gate list gls[step_gl[s]] then normalises); grads != null receives
 // df/dconj(G) for every gate of every list in the upload layouts
-double tebd_grad(tn_mps* psi0, const std::vector<const tn_gates*>& gls,
+double tebd_grad(const tn_mps* psi0, const std::vector<const tn_gates*>& gls,
                  const std::vector<int>& step_gl, const Trunc& t, int every, int obs_site,
                  const double* obs_op, double eta, double* grads);
 

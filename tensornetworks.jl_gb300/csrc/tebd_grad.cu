@@ -528,7 +528,7 @@ struct MpsOwner {
 }  // namespace
 
 // f = <psi|O|psi>/<psi|psi> after the steps; gate cotangents when grads != null
-double tebd_grad(tn_mps* psi0, const std::vector<const tn_gates*>& gls,
+double tebd_grad(const tn_mps* psi0, const std::vector<const tn_gates*>& gls,
                  const std::vector<int>& step_gl, const Trunc& t, int every, int obs_site,
                  const double* obs_op, double eta, double* grads) {
     Ctx* ctx = psi0->ctx;

@@ -91,7 +91,7 @@ _SIGS = {
     "tn_profile_phases": (i32, [P, dp]),
 }
 
-PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "zheevd (cuSOLVER FP64)",
+PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "zheevd/zheevdx (cuSOLVER FP64)",
                 "small_apply_kernel (FP64 legs)", "heff_mid_kernel (FP32 leg)",
                 "operand conversion / partial reduction", "Lanczos vector ops",
                 "all launches (count only)")

@@ -350,10 +350,12 @@ def test_error_status_on_bad_input(tn):
     assert pg.center == 2
 
 
-def test_qjmc_ensemble_matches_per_trajectory_oracle(tn):
-    """Concurrent trajectories (3 workers) against the oracle run trajectory
-    by trajectory on the same draw rows: averaged <Z_i>(t) and jump counts."""
-    N, dt, steps, ntraj = 6, 0.05, 30, 6
+@pytest.mark.parametrize("workers,ntraj", [(3, 6), (8, 12)])
+def test_qjmc_ensemble_matches_per_trajectory_oracle(tn, workers, ntraj):
+    """Concurrent trajectories (one host worker, stream and solver each)
+    against the oracle run trajectory by trajectory on the same draw rows:
+    averaged <Z_i>(t) and jump counts."""
+    N, dt, steps = 6, 0.05, 30
     draws = np.random.default_rng(9).random((ntraj, 3 * steps + 3))
     Ho, Lo = ising_qjmc(O, N)
     zo = O.OpList(N)
@@ -375,7 +377,8 @@ def test_qjmc_ensemble_matches_per_trajectory_oracle(tn):
         zg.add("z", i)
     pg = tn.productMPS(tn.spinhalf(), ["up"] * N)
     times, out, nj = tn.qjmc_ensemble(tn.spinhalf(), pg, Hg, Lg, steps * dt, dt, zg, ntraj,
-                                      draws=draws, save=5 * dt, cutoff=1e-10, maxdim=16, workers=3)
+                                      draws=draws, save=5 * dt, cutoff=1e-10, maxdim=16,
+                                      workers=workers)
     assert list(nj) == counts and sum(counts) > 0
     assert out.shape == avg.shape and np.allclose(np.real(out), avg, atol=1e-9)
     assert len(times) == out.shape[0]
