@@ -327,7 +327,7 @@ def ours(args):
 
 
 def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=256, workers=64):
-    """BASELINE config 4 shapes: N=32 Ising chain H = sum Z Z + 0.8 sum X, jumps
+    """QJMC workload shapes: N=32 Ising chain H = sum Z Z + 0.8 sum X, jumps
     L_i = sqrt(0.1) s-_i, all-up start, dt=0.01, maxdim 64, cutoff 1e-10.  One
     trajectory is evolved `pre_steps` (untimed) so the timed steps run at grown
     bond dimension; from it, `steps` steps of one trajectory alone and of
@@ -366,7 +366,7 @@ def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=256, workers=64):
 
 
 def tebd_sample(tn, ctx, pre_steps=20, steps=4):
-    """BASELINE config 3 shapes: N=64 XXZ (J=1, Delta=0.5) + staggered field
+    """TEBD quench shapes: N=64 XXZ (J=1, Delta=0.5) + staggered field
     0.2(-1)^i, Neel start, real time, 2nd order, dt=0.05, maxdim 256, cutoff
     1e-10; `steps` timed TEBD steps after `pre_steps` untimed ones."""
     import ctypes as C

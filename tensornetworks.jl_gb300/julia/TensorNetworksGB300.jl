@@ -200,7 +200,7 @@ end
 
 function tebd(st::Sitetypes, psi::GMPS, H::OpList, dt::Number, tmax::Number, save::Number,
               observers::Vector=[]; cutoff::Float64=1e-12, maxdim::Int=0, mindim::Int=1,
-              evol::String="imag", order::Int=2, norm::Real=0.0, kwargs...)
+              evol::String="imag", order::Int=2, norm::Real=0.0, precision::Symbol=:fp64, kwargs...)
     st.dim != dim(psi) && error("Sitetypes and MPS physical dimensions do not match.")
     length(psi) != length(H) && error("OpList and MPS have different lengths.")
     gates = trotterize(st, H, dt; evol=evol, order=order)
@@ -222,9 +222,10 @@ function tebd(st::Sitetypes, psi::GMPS, H::OpList, dt::Number, tmax::Number, sav
     try
         while !converged
             ln = Ref{Float64}(0.0)
-            check(ctx, ccall((:tn_tebd_steps, libtngpu), Int32,
-                             (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ref{TruncOpts}, Ref{Float64}),
-                             ctx.h, hpsi, hg, 1, t, ln))
+            check(ctx, ccall((:tn_tebd_steps_prec, libtngpu), Int32,
+                             (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ref{TruncOpts}, Int32, Ref{Float64}),
+                             ctx.h, hpsi, hg, 1, t,
+                             precision == :mixed ? TN_PREC_MIXED : TN_PREC_FP64, ln))
             normal += ln[]
             step += 1
             converged = step >= nsteps
@@ -279,6 +280,71 @@ function qjmc_simulation(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, t
         ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
     end
     return Int.(jumps[1:nj[]]), jtimes[1:nj[]]
+end
+
+# ---- differentiated TEBD: value and gradient for an rrule ---------------------
+# Segment k runs nsub TEBD steps with the Trotter gates of H_of(hs[k]) (H_of
+# affine in its argument); the objective is <op at site> of the final state.
+# The library returns df/dconj(G) for every uploaded gate; the chain to h
+# uses the Frechet derivative of exp, the upper-right block of
+# exp([A E; 0 A]) with A = tau * g and E = tau * dg/dh.
+function frechet_exp(g::Array{ComplexF64}, dg::Array{ComplexF64}, tau::Number)
+    n = ndims(g) ÷ 2
+    d = size(g, 1)
+    perm = vcat(collect(1:2:2n), collect(2:2:2n))
+    A = reshape(permutedims(tau .* g, perm), d^n, d^n)
+    E = reshape(permutedims(tau .* dg, perm), d^n, d^n)
+    L = exp([A E; zero(A) A])[1:d^n, d^n+1:end]
+    return permutedims(reshape(L, ntuple(_ -> d, 2n)), invperm(perm))
+end
+
+function tebd_objective_grad(st::Sitetypes, psi0::GMPS, H_of, hs::Vector{Float64}, dt::Real,
+                             nsub::Integer, opname::String, site::Integer; cutoff::Real=1e-12,
+                             maxdim::Int=0, mindim::Int=1, evol::String="real", checkpoint::Int=10,
+                             broadening::Real=1e-32)
+    ctx = context()
+    lists = [trotterize(st, H_of(h), dt; evol=evol, order=2) for h in hs]
+    handles = [upload_gates(ctx, gl, dim(psi0)) for gl in lists]
+    hpsi = upload(ctx, psi0)
+    steps = Int32.(repeat(0:length(hs)-1, inner=nsub))
+    ngate = sum(length(g) for gl in lists for r in gl.gates for g in r)
+    gbar = zeros(Float64, 2 * ngate)
+    f = Ref{Float64}(0.0)
+    o = convert(Array{ComplexF64}, op(st, opname))
+    try
+        check(ctx, ccall((:tn_tebd_grad, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Int32, Ptr{Int32},
+                          Ref{TruncOpts}, Int32, Int32, Ptr{ComplexF64}, Float64, Ref{Float64},
+                          Ptr{Float64}),
+                         ctx.h, hpsi, length(handles), handles, length(steps), steps,
+                         TruncOpts(cutoff, maxdim, mindim), checkpoint, site, o, broadening, f, gbar))
+    finally
+        destroy_mps(hpsi)
+        for h in handles
+            ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), h)
+        end
+    end
+    gz = reinterpret(ComplexF64, gbar)
+    dh = zeros(length(hs))
+    off = 0
+    tfac = evol == "real" ? -im * dt : dt
+    for (k, h) in enumerate(hs)
+        H0, H1 = H_of(h), H_of(h + 1.0)
+        gl = lists[k]
+        rng = TensorNetworks.siterange(H0)
+        for (r, (sites, gates)) in enumerate(zip(gl.sites, gl.gates))
+            tau = (r == rng || length(gl.gates) == 1) ? tfac : tfac / 2  # 2nd order: half steps on the outer rows
+            for (s, G) in zip(sites, gates)
+                g0 = TensorNetworks.sitetensor(H0, st, s)
+                g1 = TensorNetworks.sitetensor(H1, st, s)
+                dG = frechet_exp(convert(Array{ComplexF64}, g0), convert(Array{ComplexF64}, g1 .- g0), tau)
+                gb = reshape(gz[off+1:off+length(G)], size(G))
+                dh[k] += real(sum(conj.(gb) .* dG))
+                off += length(G)
+            end
+        end
+    end
+    return f[], dh
 end
 
 end # module

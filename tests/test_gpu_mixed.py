@@ -92,7 +92,7 @@ def test_dmrg_mixed_matches_fp64(tn):
     pmx = tn.GMPS.from_tensors(po.tensors, po.center)
     st = {}
     _, Emx = tn.dmrg(pmx, W, precision="mixed", stats=st, **kw)
-    # spec bound: |dE/E| <= 1e-9 for the FP64-recomputed energy
+    # accuracy bound: |dE/E| <= 1e-9 for the FP64-recomputed energy
     assert abs(st["energy_fp64"] - E64) <= 1e-9 * abs(E64), (st["energy_fp64"], E64, Emx)
     assert Emx == st["energy_fp64"]  # mixed mode returns the FP64 Rayleigh quotient
     # kept bond dimensions may differ by a few where sigma^2 sits at the 1e-12

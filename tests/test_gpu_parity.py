@@ -199,7 +199,7 @@ def test_inner_terms(tn):
 
 
 # ---------------------------------------------------------------------------
-# DMRG: BASELINE config 1 (TFIM N=20, D=4 start, chi<=64, 5 sweeps, Lanczos 8x2)
+# DMRG: the TFIM workload (N=20, D=4 start, chi<=64, 5 sweeps, Lanczos 8x2)
 # ---------------------------------------------------------------------------
 def tfim(mod, N, J=1.0, h=0.5):
     H = mod.OpList(N)
