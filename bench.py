@@ -259,7 +259,11 @@ def ours(args):
     tc = prof[0]
     tc_achieved = 3.0 * tc["flops"] / (tc["ms"] * 1e-3) / 1e12 if tc["ms"] > 0 else 0.0
     roof_tc = {"kernel": tc["kernel"], "bound": "tensor", "achieved": tc_achieved, "peak": tf32_peak,
-               "unit": "TFLOP/s", "frac": tc_achieved / tf32_peak, "traffic": None,
+               "unit": "TFLOP/s", "frac": tc_achieved / tf32_peak,
+               # dram bytes read + written by one bulk-shape launch (L . theta,
+               # 5120 x 4096 x 1024) in an ncu capture: 151 MB + 1282 MB
+               "traffic": 1.433e9, "traffic_note": "one ncu capture of the bulk-shape H_eff GEMM; "
+                                                   "writes are the split-K FP32 partials",
                "launches": tc["launches"], "avg_launch_ms": tc["ms"] / max(tc["launches"], 1),
                "note": "achieved counts the three TF32 passes the tensor pipe executes "
                        "(3 x 8 flops per complex multiply-add); peak = 0.5 x "
@@ -274,7 +278,11 @@ def ours(args):
         z_peak = cublas_zgemm_tflops(local)
         ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
         roof = {"kernel": dom["kernel"], "bound": "fp64-pipe", "achieved": ach, "peak": z_peak,
-                "unit": "TFLOP/s", "frac": ach / z_peak if z_peak else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": ach / z_peak if z_peak else None,
+                # dram bytes read + written by the bulk Gram launch (2048^3,
+                # lower triangle) in an ncu capture: 96 MB + 14 MB
+                "traffic": 1.106e8, "traffic_note": "one ncu capture of the bulk-shape Gram launch; "
+                                                    "the FP64 pipe is 99.6 % active",
                 "launches": dom["launches"], "avg_launch_ms": dom["ms"] / max(dom["launches"], 1),
                 "note": "peak = cuBLAS ZGEMM 4096^3 measured in this run (the measured-peaks file "
                         "has no FP64 figure)"}
