@@ -108,6 +108,55 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
     }
 }
 
+// Thin or small products (min(m, n) < 48): one thread per output element, a
+// plain dot product over k.  The 64x64 tile kernel would spend GB300's scarce
+// FP64 issue slots on zero padding there (a 10 x 10 product costs a full tile).
+template <int OPA, int OPB>
+__global__ void __launch_bounds__(64) zgemm_small_kernel(int64_t M, int64_t N, int64_t K, cplx alpha,
+                                                         const cplx* __restrict__ A, int64_t lda,
+                                                         int64_t sA, const cplx* __restrict__ B,
+                                                         int64_t ldb, int64_t sB, cplx beta,
+                                                         cplx* __restrict__ C, int64_t ldc,
+                                                         int64_t sC, int64_t batch, int lower) {
+    const int64_t total = M * N * batch;
+    const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % M, j = (idx / M) % N, b = idx / (M * N);
+        if (lower && i < j) continue;  // only the lower triangle is wanted
+        const cplx* a = A + b * sA;
+        const cplx* bb = B + b * sB;
+        cplx acc = cmk(0.0, 0.0);
+        for (int64_t l = 0; l < K; ++l) {
+            cplx x = (OPA == OP_N || OPA == OP_R) ? a[i + l * lda] : a[l + i * lda];
+            if (OPA == OP_C || OPA == OP_R) x.y = -x.y;
+            cplx y = (OPB == OP_N || OPB == OP_R) ? bb[l + j * ldb] : bb[j + l * ldb];
+            if (OPB == OP_C || OPB == OP_R) y.y = -y.y;
+            acc = cfma(x, y, acc);
+        }
+        cplx* c = C + b * sC + i + j * ldc;
+        cplx v = cmul(alpha, acc);
+        if (use_beta) v = cfma(beta, *c, v);
+        *c = v;
+    }
+}
+
+template <int OPA>
+void zgemm_small_dispatch_b(Ctx* ctx, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha,
+                            const cplx* A, int64_t lda, int64_t sA, const cplx* B, int64_t ldb,
+                            int64_t sB, cplx beta, cplx* C, int64_t ldc, int64_t sC, int64_t batch,
+                            int lower) {
+    int64_t blocks = (m * n * batch + 63) / 64;
+    const int64_t cap = (int64_t)ctx->sm_count * 16;
+    if (blocks > cap) blocks = cap;
+    const unsigned g = (unsigned)(blocks < 1 ? 1 : blocks);
+    switch (opb) {
+#define TN_ZS(OB) case OB: zgemm_small_kernel<OPA, OB><<<g, 64, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, lower); break;
+        TN_ZS(OP_N) TN_ZS(OP_T) TN_ZS(OP_C) TN_ZS(OP_R)
+#undef TN_ZS
+    }
+}
+
 template <int OPA>
 void zgemm_dispatch_b(Ctx* ctx, Op opb, dim3 grid, int64_t m, int64_t n, int64_t k, cplx alpha,
                       const cplx* A, int64_t lda, int64_t sA, const cplx* B, int64_t ldb,
@@ -476,6 +525,17 @@ void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha
     }
     ProfScope ps(ctx, 1, (lower ? 0.5 : 1.0) * 8.0 * m * n * (double)std::max<int64_t>(k, 0) * batch,
                  16.0 * (double)(m * k + k * n + m * n) * batch);
+    if (std::min(m, n) < 48) {
+        switch (opa) {
+            case OP_N: zgemm_small_dispatch_b<OP_N>(ctx, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, lower); break;
+            case OP_T: zgemm_small_dispatch_b<OP_T>(ctx, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, lower); break;
+            case OP_C: zgemm_small_dispatch_b<OP_C>(ctx, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, lower); break;
+            case OP_R: zgemm_small_dispatch_b<OP_R>(ctx, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, lower); break;
+        }
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+        return;
+    }
     switch (opa) {
         case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
         case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
