@@ -155,6 +155,18 @@ __host__ __device__ inline cplx cfma(cplx a, cplx b, cplx c) {  // a*b + c
     return cmk(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
 }
 
+// hi + lo += v in float-float arithmetic: hi takes the rounded sum, lo the
+// exact rounding error (Knuth's TwoSum; additions only, so no contraction).
+// Summing FP32 partials this way keeps ~46 bits without FP64 instructions,
+// which GB300 issues at a small fraction of the FP32 rate.
+__host__ __device__ inline void ff_add(float& hi, float& lo, float v) {
+    const float t = hi + v;
+    const float bp = t - hi;
+    const float e = (hi - (t - bp)) + (v - bp);
+    hi = t;
+    lo += e;
+}
+
 // ---- kernels (kernels_fp64.cu) -----------------------------------------
 enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };  // R: conjugate without transpose
 

@@ -101,13 +101,13 @@ __global__ void __launch_bounds__(256) heff_mid_kernel(
             // I = w + wl*(s1 + d*s2); T1 row (a + cl*w), column (s1 + d*s2 + d2*c)
             const int w = I % wl, s12 = I / wl;
             const int64_t off = (a + cl * w) + ldt1 * (s12 + (int64_t)d2 * c);
-            // sum the K-chunk partials of GEMM1 (FP64 sum, then FP32)
-            double sr = 0.0, si = 0.0;
+            // sum the K-chunk partials of GEMM1 in float-float, then round
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
             for (int z = 0; z < S1; ++z) {
-                sr += (double)t1r[(size_t)z * chunk1 + off];
-                si += (double)t1i[(size_t)z * chunk1 + off];
+                ff_add(rh, rl, t1r[(size_t)z * chunk1 + off]);
+                ff_add(ih, il, t1i[(size_t)z * chunk1 + off]);
             }
-            const float xr = (float)sr, xi = (float)si;
+            const float xr = rh + rl, xi = ih + il;
 #pragma unroll
             for (int J = 0; J < MID_MAXJ; ++J) {
                 if (J < nJ) {
@@ -124,18 +124,23 @@ __global__ void __launch_bounds__(256) heff_mid_kernel(
     __syncthreads();
     // rows (a, s1', s2') x columns (w'' + wr*c) for this block's c range
     const size_t plane = (size_t)rows2 * ld2;
-    const int ncol = wr * MID_C;
+    // each thread keeps one column (w'', c) and walks rows: the divisions by
+    // wr happen once per thread, the row split is by the power-of-two MID_A
+    const int ncol = wr * MID_C;  // <= 64: d2 * wr <= MID_MAXJ
     const int nrow = MID_A * d2;
-    for (int e = threadIdx.x; e < nrow * ncol; e += blockDim.x) {
-        const int col = e % ncol, row = e / ncol;
+    const int rpp = blockDim.x / ncol;  // rows per pass
+    const int tcol = threadIdx.x % ncol, trow = threadIdx.x / ncol;
+    if (trow >= rpp) return;
+    const int w2 = tcol % wr, cloc = tcol / wr;
+    const int64_t cg = (int64_t)blockIdx.y * MID_C + cloc;
+    if (cg >= cr) return;
+    const int64_t Kc = w2 + (int64_t)wr * cg;
+    for (int row = trow; row < nrow; row += rpp) {
         const int al = row % MID_A, s12 = row / MID_A;
-        const int w2 = col % wr, cloc = col / wr;
         const int64_t ag = (int64_t)blockIdx.x * MID_A + al;
-        const int64_t cg = (int64_t)blockIdx.y * MID_C + cloc;
-        if (ag >= cl || cg >= cr) continue;
+        if (ag >= cl) continue;
         const float2 v = sY[(cloc * MID_A + al) * nJ + (s12 + d2 * w2)];
         const int64_t R = ag + cl * s12;
-        const int64_t Kc = w2 + (int64_t)wr * cg;
         const size_t off = (size_t)R * ld2 + Kc;
         const float rh = to_tf32(v.x), ih = to_tf32(v.y);
         planes[off] = rh;
@@ -178,12 +183,12 @@ __global__ void __launch_bounds__(128) env_left_leg_kernel(
         if (I < nI) {
             const int w = I % wl, s = I / wl;
             const int64_t off = (a + ca * w) + M * (s + (int64_t)d * bp);
-            double sr = 0.0, si = 0.0;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
             for (int z = 0; z < S; ++z) {
-                sr += (double)P[(size_t)z * chunk + off];
-                si += (double)P[(size_t)z * chunk + plane_in + off];
+                ff_add(rh, rl, P[(size_t)z * chunk + off]);
+                ff_add(ih, il, P[(size_t)z * chunk + plane_in + off]);
             }
-            x[I] = make_float2((float)sr, (float)si);
+            x[I] = make_float2(rh + rl, ih + il);
         }
     }
     const size_t plane = (size_t)rows * ld;
@@ -226,12 +231,12 @@ __global__ void __launch_bounds__(256) env_right_leg_kernel(
         if (I < nI && a < ca && bp < cb2) {
             const int sp = I % d, wp = I / d;
             const int64_t off = (a + ca * sp) + M * (wp + (int64_t)wr * bp);
-            double sr = 0.0, si = 0.0;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
             for (int z = 0; z < S; ++z) {
-                sr += (double)P[(size_t)z * chunk + off];
-                si += (double)P[(size_t)z * chunk + plane_in + off];
+                ff_add(rh, rl, P[(size_t)z * chunk + off]);
+                ff_add(ih, il, P[(size_t)z * chunk + plane_in + off]);
             }
-            x[I] = make_float2((float)sr, (float)si);
+            x[I] = make_float2(rh + rl, ih + il);
         }
     }
     for (int J = 0; J < nJ; ++J) {

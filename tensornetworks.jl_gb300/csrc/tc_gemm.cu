@@ -371,11 +371,12 @@ __global__ void reduce_partials_fp64_kernel(const float* __restrict__ P, int S, 
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t m = i % M, n = i / M;
         const int64_t off = m + ldp * n;
-        double re = 0.0, im = 0.0;
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
         for (int z = 0; z < S; ++z) {
-            re += (double)P[(size_t)z * chunk + off];
-            im += (double)P[(size_t)z * chunk + plane + off];
+            ff_add(rh, rl, P[(size_t)z * chunk + off]);
+            ff_add(ih, il, P[(size_t)z * chunk + plane + off]);
         }
+        double re = (double)rh + (double)rl, im = (double)ih + (double)il;
         cplx* o = out + m + ldo * n;
         if (accumulate) {
             re += o->x;
