@@ -131,6 +131,34 @@ def test_truncate_keep_rule_and_factors(tn, case, direction):
         assert np.allclose(Yg @ Yg.conj().T, np.eye(kk), atol=1e-12)
 
 
+@pytest.mark.parametrize("direction", [0, 1])
+@pytest.mark.parametrize("m,n", [(150, 300), (300, 150)])
+def test_truncate_rectangular_top_k(tn, m, n, direction):
+    """Rectangular splits on the top-eigenpair path: the Gram order is the
+    isometric side (m or n) and exceeds the kept count."""
+    ctx = tn.context()
+    rng = np.random.default_rng(m + 2 * n + direction)
+    S = np.geomspace(1, 1e-9, min(m, n))
+    M = _matrix_with_spectrum(rng, m, n, S)
+    cutoff, maxdim = 1e-12, 60
+    U, So, Vt = O.trunc_svd(M, cutoff, maxdim, 1)
+    k = C.c_int64(min(m, n))
+    Xo = np.zeros((m, min(m, n)), dtype=np.complex128, order="F")
+    Yo = np.zeros((min(m, n), n), dtype=np.complex128, order="F")
+    Sg = np.zeros(min(m, n))
+    t = tn._lib.trunc(cutoff, maxdim, 1)
+    ctx.check(ctx.lib.tn_truncate(ctx.h, m, n, dp(M), C.byref(t), direction, dp(Xo), dp(Yo), dp(Sg),
+                                  C.byref(k)))
+    kk = k.value
+    assert kk == So.size == maxdim
+    Xg = np.asfortranarray(Xo.ravel(order="F")[: m * kk].reshape((m, kk), order="F"))
+    Yg = np.asfortranarray(Yo.ravel(order="F")[: kk * n].reshape((kk, n), order="F"))
+    assert np.allclose(Sg[:kk], So, atol=1e-9)
+    assert np.allclose(Xg @ Yg, (U * So) @ Vt, atol=1e-9)
+    iso = Xg.conj().T @ Xg if direction == 0 else Yg @ Yg.conj().T
+    assert np.allclose(iso, np.eye(kk), atol=1e-12)
+
+
 # ---------------------------------------------------------------------------
 # MPS operations
 # ---------------------------------------------------------------------------
