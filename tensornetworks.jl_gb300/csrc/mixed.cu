@@ -345,7 +345,7 @@ void heff2_planes(Ctx* ctx, MixedWork& B, const cplx* W12, int64_t cl, int64_t c
                                                       t2.ld, t2.rows);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
-    // out = T2 * R^T, partials summed in FP64 into [(a s1' s2'), c']
+    // out = T2 * R^T, partials summed in float-float into FP64 [(a s1' s2'), c']
     const int64_t M3 = cl * d2, N3 = cr;
     const int S3 = tc_chunks(wr * cr);
     const int64_t chunk3 = 2 * M3 * N3;

@@ -361,7 +361,7 @@ int tc_cgemm_partials(Ctx* ctx, const TcPlanes& A, const TcPlanes& B, int64_t M,
 }
 
 namespace {
-// out[m + ldo*n] (+)= sum_z P[z][re|im][m + ldp*n], summed in FP64
+// out[m + ldo*n] (+)= sum_z P[z][re|im][m + ldp*n], summed in float-float (TwoSum), stored as FP64
 __global__ void reduce_partials_fp64_kernel(const float* __restrict__ P, int S, int64_t M,
                                             int64_t N, int64_t ldp, int64_t plane,
                                             int64_t chunk, cplx* __restrict__ out, int64_t ldo,
