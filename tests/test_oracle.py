@@ -217,3 +217,33 @@ def test_qjmc_matches_lindblad():
         ex = np.real(np.trace(rho @ X.oplist_to_dense(st, _single(N, "z", i))))
         err = zs[:, i - 1].std() / np.sqrt(ntraj)
         assert abs(zs[:, i - 1].mean() - ex) < 4 * err + 0.03
+
+
+def test_tebd_xx_chain_matches_free_fermion_dynamics():
+    """Beyond exact-diagonalisation sizes: the XX chain H = sum (X X + Y Y)
+    maps (Jordan-Wigner) to free fermions with hopping 2, so <Z_i>(t) from
+    a Neel state follows from the single-particle propagator exp(-i h t).
+    The oracle's real-time TEBD (N=24, chi<=64, dt=0.01) must agree up to
+    its second-order Trotter error."""
+    import scipy.linalg as sla
+    st = O.spinhalf()
+    N, dt, steps = 24, 0.01, 50
+    H = xxz(N, 1.0, 0.0)
+    names = ["up" if i % 2 else "dn" for i in range(1, N + 1)]
+    psi = O.product_mps(st, names)
+    zops = O.OpList(N)
+    for i in range(1, N + 1):
+        zops.add("z", i)
+    rec = {}
+    O.tebd(st, psi, H, dt, steps * dt, steps * dt, [zops], cutoff=1e-12, maxdim=64, evol="real",
+           record=rec)
+    z_tebd = np.real(np.asarray(rec["ops"][-1][0]))
+    # free fermions: n_i = (1 + Z_i) / 2 with "up" occupied; C(t) = U C(0) U^H
+    h = 2.0 * (np.eye(N, k=1) + np.eye(N, k=-1))
+    U = sla.expm(-1j * h * steps * dt)
+    n0 = np.array([1.0 if i % 2 else 0.0 for i in range(1, N + 1)])
+    C = U @ np.diag(n0) @ U.conj().T
+    z_exact = 2.0 * np.real(np.diag(C)) - 1.0
+    assert np.max(np.abs(z_tebd - z_exact)) < 2e-4, np.max(np.abs(z_tebd - z_exact))  # 4e-5 measured
+    # and the dynamics is far from trivial at this time
+    assert np.max(np.abs(z_exact - (2.0 * n0 - 1.0))) > 0.5
