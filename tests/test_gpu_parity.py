@@ -312,6 +312,29 @@ def test_tebd_quench_parity(tn):
     assert abs(pg.entropy(N // 2) - po.entropy(N // 2)) < 1e-9
 
 
+def test_tebd_xx_chain_n64_matches_free_fermion_dynamics(tn):
+    """The TEBD quench at the N=64 size, against an exact answer: the XX
+    chain (delta=0) is free fermions with hopping 2, so <Z_i>(t) from a Neel
+    state follows from the single-particle propagator.  Agreement up to the
+    second-order Trotter error (4e-5 at N=24 for the same dt and t)."""
+    import scipy.linalg as sla
+    N, dt, steps = 64, 0.01, 50
+    names = ["up" if i % 2 else "dn" for i in range(1, N + 1)]
+    zg = tn.OpList(N)
+    for i in range(1, N + 1):
+        zg.add("z", i)
+    pg = tn.productMPS(tn.spinhalf(), names)
+    ob = tn.TEBDOperators(tn.spinhalf(), zg)
+    tn.tebd(tn.spinhalf(), pg, xxz(tn, N, 1.0, 0.0), dt, steps * dt, steps * dt, [ob],
+            cutoff=1e-12, maxdim=64, evol="real")
+    z_gpu = np.real(np.asarray(ob.measurements[-1]))
+    h = 2.0 * (np.eye(N, k=1) + np.eye(N, k=-1))
+    U = sla.expm(-1j * h * steps * dt)
+    n0 = np.array([1.0 if i % 2 else 0.0 for i in range(1, N + 1)])
+    z_exact = 2.0 * np.real(np.diag(U @ np.diag(n0) @ U.conj().T)) - 1.0
+    assert np.max(np.abs(z_gpu - z_exact)) < 2e-4, np.max(np.abs(z_gpu - z_exact))
+
+
 def test_tebd_imaginary_time_ground_state(tn):
     # evol="imag" applies exp(+dt H) (gatelist.jl:87,100): pass -H to target
     # the ground state, as the reference's users do
