@@ -247,3 +247,20 @@ def test_tebd_xx_chain_matches_free_fermion_dynamics():
     assert np.max(np.abs(z_tebd - z_exact)) < 2e-4, np.max(np.abs(z_tebd - z_exact))  # 4e-5 measured
     # and the dynamics is far from trivial at this time
     assert np.max(np.abs(z_exact - (2.0 * n0 - 1.0))) > 0.5
+
+
+def test_dmrg_xx_chain_free_fermion_energy():
+    """Oracle DMRG beyond exact-diagonalisation sizes: the XX chain at N=32
+    (free fermions with hopping 2, single-particle energies 4 cos(k pi/(N+1)))
+    has ground energy = sum of the negative single-particle energies."""
+    N = 32
+    rng = np.random.default_rng(8)
+    shapes = [((1 if i == 0 else 8), 2, (1 if i == N - 1 else 8)) for i in range(N)]
+    draws = [O.fr(rng.standard_normal(int(np.prod(s))), s) for s in shapes]
+    draws.append(O.fr(rng.standard_normal(4), (1, 2, 2)))
+    psi = O.random_mps(2, N, 8, draws)
+    H = O.mpo_from_oplist(O.spinhalf(), xxz(N, 1.0, 0.0))
+    _, E = O.dmrg(psi, H, maxdim=48, cutoff=1e-12, minsweeps=6, maxsweeps=6, numconverges=np.inf)
+    eps = 4.0 * np.cos(np.arange(1, N + 1) * np.pi / (N + 1))
+    E_exact = float(np.sum(eps[eps < 0]))
+    assert abs(np.real(E) - E_exact) <= 1e-6 * abs(E_exact), (np.real(E), E_exact)
