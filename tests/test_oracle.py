@@ -1,11 +1,21 @@
 """Pins the CPU oracle against known-answer physics (the reference ships no
 golden vectors: test/runtests.jl is an empty testset)."""
 
+import json
+import os
+
 import numpy as np
 import pytest
 
 import oracle as O
 from oracle import exact as X
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def known_answers():
+    with open(os.path.join(GOLDEN, "known_answers.json")) as f:
+        return json.load(f)
 
 
 def tfim(N, J=1.0, h=0.5):
@@ -225,7 +235,6 @@ def test_tebd_xx_chain_matches_free_fermion_dynamics():
     a Neel state follows from the single-particle propagator exp(-i h t).
     The oracle's real-time TEBD (N=24, chi<=64, dt=0.01) must agree up to
     its second-order Trotter error."""
-    import scipy.linalg as sla
     st = O.spinhalf()
     N, dt, steps = 24, 0.01, 50
     H = xxz(N, 1.0, 0.0)
@@ -239,11 +248,8 @@ def test_tebd_xx_chain_matches_free_fermion_dynamics():
            record=rec)
     z_tebd = np.real(np.asarray(rec["ops"][-1][0]))
     # free fermions: n_i = (1 + Z_i) / 2 with "up" occupied; C(t) = U C(0) U^H
-    h = 2.0 * (np.eye(N, k=1) + np.eye(N, k=-1))
-    U = sla.expm(-1j * h * steps * dt)
+    z_exact = np.asarray(known_answers()["xx_open_N24_neel_t0.5_z"])
     n0 = np.array([1.0 if i % 2 else 0.0 for i in range(1, N + 1)])
-    C = U @ np.diag(n0) @ U.conj().T
-    z_exact = 2.0 * np.real(np.diag(C)) - 1.0
     assert np.max(np.abs(z_tebd - z_exact)) < 2e-4, np.max(np.abs(z_tebd - z_exact))  # 4e-5 measured
     # and the dynamics is far from trivial at this time
     assert np.max(np.abs(z_exact - (2.0 * n0 - 1.0))) > 0.5
@@ -261,6 +267,19 @@ def test_dmrg_xx_chain_free_fermion_energy():
     psi = O.random_mps(2, N, 8, draws)
     H = O.mpo_from_oplist(O.spinhalf(), xxz(N, 1.0, 0.0))
     _, E = O.dmrg(psi, H, maxdim=48, cutoff=1e-12, minsweeps=6, maxsweeps=6, numconverges=np.inf)
-    eps = 4.0 * np.cos(np.arange(1, N + 1) * np.pi / (N + 1))
-    E_exact = float(np.sum(eps[eps < 0]))
+    E_exact = known_answers()["xx_open_N32_energy"]
     assert abs(np.real(E) - E_exact) <= 1e-6 * abs(E_exact), (np.real(E), E_exact)
+
+
+def test_known_answer_fixtures_are_current():
+    """tests/golden/known_answers.json equals what its generating script
+    computes, and its TFIM value equals the oracle's free-fermion helper."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    fresh, stored = m.answers(), known_answers()
+    assert set(fresh) == set(stored)
+    for k in fresh:
+        assert np.allclose(fresh[k], stored[k], rtol=1e-13, atol=1e-13), k
+    assert abs(stored["tfim_open_N20_J1_h0.5_energy"] - X.tfim_free_fermion_energy(20, 1.0, 0.5)) < 1e-12
