@@ -14,4 +14,5 @@ from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEB
                          qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation, shard_range, tebd,
                          tebd_grad, trotterize)
 from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
-from .mps import GMPS, MPO, MPOHandle, entropy, inner, productMPS, randomMPS  # noqa: F401
+from .mps import (GMPS, MPO, MPOHandle, entropy, inner, mps_from_record, mps_record,  # noqa: F401
+                  productMPS, randomMPS, read_mps, write_mps)

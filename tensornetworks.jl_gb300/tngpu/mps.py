@@ -230,3 +230,39 @@ def normalize(psi):
 
 def movecenter(psi, idx, **kw):
     psi.movecenter(idx, **kw)
+
+
+# ---------------------------------------------------------------------------
+# Checkpoints (the GMPS HDF5 group of gmps.jl:359-383, as an .npz archive:
+# h5py is not a dependency).  The group's fields keep their names and
+# meaning: attributes type="MPS" and version=1, datasets "length", "center"
+# and "MPS[i]" (1-based, [Dl, d, Dr] complex).
+# ---------------------------------------------------------------------------
+def mps_record(tensors, center, name="psi"):
+    """The archive entries of one MPS group."""
+    rec = {f"{name}/type": np.array("MPS"), f"{name}/version": np.array(1),
+           f"{name}/length": np.array(len(tensors)), f"{name}/center": np.array(int(center))}
+    for i, t in enumerate(tensors, start=1):
+        rec[f"{name}/MPS[{i}]"] = np.asarray(t, dtype=np.complex128)
+    return rec
+
+
+def mps_from_record(rec, name="psi"):
+    """(tensors, center) of one MPS group; the reference's read check."""
+    key = f"{name}/type"
+    if key not in rec or str(rec[key]) != "MPS":
+        raise ValueError("HDF5 group of file does not contain MPS data.")
+    N = int(rec[f"{name}/length"])
+    return [np.asarray(rec[f"{name}/MPS[{i}]"]) for i in range(1, N + 1)], int(rec[f"{name}/center"])
+
+
+def write_mps(path, psi, name="psi"):
+    """Download psi and store it as the group ``name`` of an .npz archive."""
+    np.savez(path, **mps_record(psi.tensors(), psi.center, name))
+
+
+def read_mps(path, name="psi", ctx=None):
+    """Upload the MPS group ``name`` of an archive written by write_mps."""
+    with np.load(path, allow_pickle=False) as z:
+        tensors, center = mps_from_record({k: z[k] for k in z.files}, name)
+    return GMPS.from_tensors(tensors, center, ctx)

@@ -143,3 +143,24 @@ def test_product_path_does_not_import_oracle():
     for f in os.listdir(pkg):
         if f.endswith(".py"):
             assert "oracle" not in open(os.path.join(pkg, f)).read(), f
+
+
+def test_mps_checkpoint_record_round_trip(tmp_path):
+    """The checkpoint layout (gmps.jl:359-383 field names) survives an .npz
+    round trip, and a group of another type is rejected with the reference's
+    message."""
+    import tngpu.mps as M
+    rng = np.random.default_rng(3)
+    ts = [rng.standard_normal((1, 2, 3)) + 1j * rng.standard_normal((1, 2, 3)),
+          rng.standard_normal((3, 2, 1)) + 0j]
+    rec = M.mps_record(ts, 2, name="state")
+    path = tmp_path / "ck.npz"
+    np.savez(path, **rec)
+    with np.load(path, allow_pickle=False) as z:
+        back, center = M.mps_from_record({k: z[k] for k in z.files}, name="state")
+    assert center == 2 and len(back) == 2
+    assert all(np.array_equal(a, b) for a, b in zip(ts, back))
+    bad = dict(rec)
+    bad["state/type"] = np.array("MPO")
+    with pytest.raises(ValueError, match="does not contain MPS data"):
+        M.mps_from_record(bad, name="state")
