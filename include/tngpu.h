@@ -228,16 +228,19 @@ int32_t tn_heff2_apply(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64
                        int64_t wr, const double* L, const double* W1, const double* W2,
                        const double* R, const double* theta, double* out, int32_t precision);
 /* The same product as tn_heff2_apply (FP64) for callers that cannot allocate
- * device memory: hosts that run inside a device-memory budget of their own
- * and hand the library buffers from their arena, or loops where an
- * allocation's implicit synchronisation is not allowed.  Every pointer
- * (L, W1, W2, R, theta, out) is a DEVICE pointer the caller owns; nothing is
- * allocated.  Intermediates live in one static 64 MiB device array that the
- * library holds on every GPU that loads it, until exit; problems needing
- * more (16*chil*chir*d^2*(wl+wr) bytes plus the merged operator) are
- * rejected with TN_ERR_INVALID.  All calls share that array: calls whose GPU
- * work overlaps race and must be serialised by the caller.  The first call on
- * a device resolves the array's address; make it before any stream capture.
+ * device memory: a host that owns the GPU's memory through its own arena and
+ * budget and hands the library buffers from it, or a long run that must not
+ * stop on an out-of-memory error halfway.  Every pointer (L, W1, W2, R,
+ * theta, out) is a DEVICE pointer on the context's GPU that the caller owns;
+ * nothing is allocated.  Intermediates live in one static 64 MiB device
+ * array that the library holds on every GPU that loads it, until exit;
+ * problems needing more (16*chil*chir*d^2*(wl+wr) bytes plus the merged
+ * operator), or a merged operator (wl*d^2)*(d^2*wr) above 4096 entries, are
+ * rejected with TN_ERR_INVALID.  All calls share that array and it keeps the
+ * last call's contents: calls whose GPU work overlaps race and must be
+ * serialised by the caller.  As every entry point, the call returns after its
+ * work has finished.  The first call on a device resolves the array's
+ * address; make it before any stream capture.
  * No counterpart in the reference: an addition for allocation-free callers. */
 int32_t tn_heff2_apply_noalloc(tn_ctx* ctx, int64_t chil, int64_t chir, int32_t d, int64_t wl,
                                int64_t wm, int64_t wr, const double* L, const double* W1,
@@ -265,6 +268,15 @@ int32_t tn_gemm(tn_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, i
 int32_t tn_truncate(tn_ctx* ctx, int64_t m, int64_t n, const double* theta,
                     const tn_trunc_opts* trunc, int32_t direction, double* X, double* Y,
                     double* S, int64_t* k);
+
+/* Top `want` eigenpairs of the Hermitian n x n matrix G (host, interleaved,
+ * column-major; the lower triangle is read): lam[g] is the g-th largest
+ * eigenvalue, V[:, g] (n x want) its unit eigenvector.  The library's own
+ * FP64 eigensolver (Householder tridiagonalisation, bisection, inverse
+ * iteration, QR re-orthonormalisation, back-transformation), which sets the
+ * cut of every truncated split in place of LAPACK's SVD at tensors.jl:191-195;
+ * exposed for tests and callers.  n <= 4096. */
+int32_t tn_eigh_top(tn_ctx* ctx, int64_t n, const double* G, int64_t want, double* lam, double* V);
 
 #ifdef __cplusplus
 }

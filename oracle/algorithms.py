@@ -364,11 +364,17 @@ class UniformStream:
 
 
 def qjmc_simulation(st, psi, H, jumpops, tmax, dt, rand, observers=None, save=0.0,
-                    cutoff=1e-12, mindim=1, maxdim=0, classical=True, record=None):
+                    cutoff=1e-12, mindim=1, maxdim=0, classical=True, record=None,
+                    entropies=False):
     """One trajectory (qjmc.jl:28-166).  ``rand`` is a callable returning the
     next uniform draw; per step the reference draws once unconditionally
     (qjmc.jl:64), once for the jump decision (:97) and once more on a jump
-    (:99).  Returns (jumps, jumptimes) with 1-based jump indices."""
+    (:99).  Returns (jumps, jumptimes) with 1-based jump indices.
+
+    ``entropies=True`` also records, at every save, the entanglement entropy
+    at every bond 1..N-1 as QJMCEntropy does (qjmc.jl:301-309): each
+    entropy(psi, i) moves the centre to i (gmps.jl:184-189), so the
+    measurement changes the gauge the next steps start from."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -381,6 +387,9 @@ def qjmc_simulation(st, psi, H, jumpops, tmax, dt, rand, observers=None, save=0.
         if record is not None:
             record.setdefault("times", []).append(tt)
             record.setdefault("ops", []).append([inner(st, psi, o, psi) for o in observers])
+            if entropies:
+                record.setdefault("entropy", []).append(
+                    [psi.entropy(b) for b in range(1, len(psi))])
 
     measure(t)
     N = len(psi)

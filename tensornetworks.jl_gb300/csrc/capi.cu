@@ -819,4 +819,27 @@ int32_t tn_truncate(tn_ctx* h, int64_t m, int64_t n, const double* theta, const 
     TN_API_END
 }
 
+int32_t tn_eigh_top(tn_ctx* h, int64_t n, const double* G, int64_t want, double* lam,
+                    double* V) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(G && lam && V, "null argument");
+    TN_REQUIRE(n >= 1 && want >= 1 && want <= n, "bad dimensions");
+    Ctx* ctx = &h->c;
+    DBuf dG(ctx, 16 * (size_t)n * n), dV(ctx, 16 * (size_t)n * want), dL(ctx, 8 * (size_t)want);
+    h2d(ctx, dG.p, G, 16 * (size_t)n * n);
+    eig_top(ctx, dG.c(), n, want, dL.d(), dV.c());
+    std::vector<double> asc(want);
+    d2h(ctx, asc.data(), dL.p, 8 * (size_t)want);
+    d2h(ctx, V, dV.p, 16 * (size_t)n * want);
+    int herr = 0;
+    d2h(ctx, &herr, ctx->d_bar + 2, sizeof(int));
+    ctx->sync();
+    if (herr) {
+        TN_CHECK_CUDA(cudaMemsetAsync(ctx->d_bar + 2, 0, sizeof(unsigned), ctx->stream));
+        throw Error(TN_ERR_TIMEOUT, "eigensolver: a bounded grid barrier ran out");
+    }
+    for (int64_t g = 0; g < want; ++g) lam[g] = asc[want - 1 - g];
+    TN_API_END
+}
+
 }  // extern "C"

@@ -2,7 +2,6 @@
 #pragma once
 
 #include <cuda_runtime.h>
-#include <cusolverDn.h>
 #include <stdint.h>
 
 #include <cstdio>
@@ -28,14 +27,6 @@ struct Error : public std::runtime_error {
         if (_e != cudaSuccess)                                                       \
             throw ::tn::Error(_e == cudaErrorMemoryAllocation ? TN_ERR_OOM : TN_ERR_CUDA, \
                               std::string(#expr) + ": " + cudaGetErrorString(_e));   \
-    } while (0)
-
-#define TN_CHECK_SOLVER(expr)                                                        \
-    do {                                                                             \
-        cusolverStatus_t _s = (expr);                                                \
-        if (_s != CUSOLVER_STATUS_SUCCESS)                                           \
-            throw ::tn::Error(TN_ERR_CUDA, std::string(#expr) + ": cusolver status " + \
-                              std::to_string((int)_s));                             \
     } while (0)
 
 #define TN_REQUIRE(cond, msg)                                                        \
@@ -74,14 +65,16 @@ struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaMemPool_t pool = nullptr;
-    cusolverDnHandle_t solver = nullptr;
     std::string err;
     int64_t launches = 0;
     int sm_count = 0;
     // reusable scratch for the hot path
     Scratch s_gram, s_eigval, s_work, s_x, s_y, s_t1, s_t2, s_dot, s_coef, s_mixa, s_mixb, s_mixc,
-        s_mixd, s_mixe, s_mixf;
+        s_mixd, s_mixe, s_mixf, s_eig;
     int* d_info = nullptr;
+    // grid-barrier words of the eigensolver's cooperative kernels: arrival
+    // count, generation, and an error word set when a bounded wait ran out
+    unsigned* d_bar = nullptr;
     int* d_err = nullptr;  // set by device code when a bounded wait runs out
     // mixed precision on: environment updates and truncation projections run
     // on the tensor cores (set for the duration of a mixed-precision sweep)
@@ -139,7 +132,7 @@ struct ProfScope {
     }
 };
 
-// stream, solver handle, pool settings and device flags of a context
+// stream, pool settings and device flags of a context
 void ctx_init(Ctx& c, int device);
 void ctx_release(Ctx& c);
 
@@ -228,10 +221,14 @@ struct SplitResult { int64_t k; double discarded; double total; };
 SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, double cutoff,
                         int64_t maxdim, int64_t mindim, bool left_iso, DBuf& X, DBuf& Y,
                         std::vector<double>* S);
-// Hermitian eigen-decomposition in place (eigenvectors overwrite G), ascending.
-// top in (0, n): only the top eigenpairs, in ascending order in dlam[0..top)
-// and the first top columns of G.  Returns the number of eigenpairs.
-// check = false: the solver status stays in ctx->d_info for the caller.
-int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top = 0, bool check = true);
+// Top `want` eigenpairs of the Hermitian n x n matrix G (lower triangle read,
+// G destroyed), hand-written FP64 kernels (eig.cu): lam_asc[want-1-g] is the
+// g-th largest eigenvalue and X[:, g] (n x want) its eigenvector.  No host
+// synchronisation; a timed-out grid barrier leaves ctx->d_bar[2] nonzero.
+void eig_top(Ctx* ctx, cplx* G, int64_t n, int64_t want, double* lam_asc, cplx* X);
+// Full eigen-decomposition, ascending: eigenvalues in dlam[0..n), eigenvectors
+// overwrite G (column j belongs to dlam[j]); synchronises and checks.
+void heev_full(Ctx* ctx, cplx* G, int64_t n, double* dlam);
+
 
 }  // namespace tn

@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
     C += bz * sC;
     const int64_t m0 = (int64_t)blockIdx.x * GB_M, n0 = (int64_t)blockIdx.y * GB_N;
     // lower: only the lower triangle is wanted (a Hermitian Gram matrix read
-    // by a LOWER-mode eigensolver); tiles strictly above the diagonal skip
+    // by the eigensolver, which reads the lower triangle); tiles strictly
+    // above the diagonal skip
     if (lower && n0 >= m0 + GB_M) return;
     cplx acc[4][4];
 #pragma unroll
@@ -552,6 +553,12 @@ void small_apply(Ctx* ctx, const cplx* in, cplx* out, const cplx* M, int nI, int
     if (na <= 0 || nc <= 0) return;
     TN_REQUIRE(nI * nJ <= 4096, "small_apply: operator too large");
     const size_t smem = sizeof(cplx) * nI * nJ;
+    // the whole operator is staged in shared memory: up to 64 KiB, above the
+    // 48 KiB a launch gets without opting in
+    if (smem > 48 * 1024)
+        TN_CHECK_CUDA(cudaFuncSetAttribute(small_apply_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(cplx) * 4096)));
     ProfScope ps(ctx, 3, 8.0 * na * nc * nI * nJ, 16.0 * na * nc * (nI + nJ));
     small_apply_kernel<<<grid_for(ctx, na * nc), 256, smem, ctx->stream>>>(
         in, out, M, nI, nJ, na, nc, lda_i, ldc_i, lda_o, ldc_o, accumulate ? 1 : 0);
@@ -710,9 +717,11 @@ KeepResult keep_rule(Ctx* ctx, const double* dlam, int64_t n, int64_t sz, double
         TN_CHECK_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(h + 3), dinfo, sizeof(int),
                                       cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    if (dinfo && *reinterpret_cast<int*>(h + 3) != 0)
-        throw Error(TN_ERR_NUMERIC, "Hermitian eigensolver failed, info = " +
-                                        std::to_string(*reinterpret_cast<int*>(h + 3)));
+    if (dinfo && *reinterpret_cast<int*>(h + 3) != 0) {
+        // the eigensolver's error word: a bounded grid barrier ran out
+        TN_CHECK_CUDA(cudaMemsetAsync(const_cast<int*>(dinfo), 0, sizeof(int), ctx->stream));
+        throw Error(TN_ERR_TIMEOUT, "eigensolver: a bounded grid barrier ran out");
+    }
     KeepDev r;
     memcpy(&r, h, sizeof(KeepDev));
     return KeepResult{r.k, r.total, r.discarded};

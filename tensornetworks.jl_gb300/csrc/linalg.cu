@@ -6,7 +6,8 @@
 // isometry is an eigenvector matrix (orthonormal to working precision) and
 // the other factor is a projection; no division by small singular values is
 // needed.  The Gram product runs on our GEMM, the Hermitian eigenproblem on
-// cuSOLVER's zheevd (FP64), and the keep rule on the warp-shuffle kernel.
+// this library's FP64 eigensolver (eig.cu), and the keep rule on the
+// warp-shuffle kernel.
 #include "common.cuh"
 #include "mixed.cuh"
 
@@ -69,9 +70,9 @@ void ctx_init(Ctx& c, int device) {
     TN_CHECK_CUDA(cudaDeviceGetDefaultMemPool(&c.pool, device));
     uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
     TN_CHECK_CUDA(cudaMemPoolSetAttribute(c.pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    TN_CHECK_SOLVER(cusolverDnCreate(&c.solver));
-    TN_CHECK_SOLVER(cusolverDnSetStream(c.solver, c.stream));
     TN_CHECK_CUDA(cudaMalloc(&c.d_info, sizeof(int)));
+    TN_CHECK_CUDA(cudaMalloc(&c.d_bar, 4 * sizeof(unsigned)));
+    TN_CHECK_CUDA(cudaMemset(c.d_bar, 0, 4 * sizeof(unsigned)));
     TN_CHECK_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
     TN_CHECK_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
     TN_CHECK_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
@@ -83,11 +84,11 @@ void ctx_release(Ctx& c) {
     // scratch buffers release through the stream before it goes away
     Scratch* all[] = {&c.s_gram, &c.s_eigval, &c.s_work, &c.s_x, &c.s_y, &c.s_t1, &c.s_t2,
                       &c.s_dot, &c.s_coef, &c.s_mixa, &c.s_mixb, &c.s_mixc, &c.s_mixd, &c.s_mixe,
-                      &c.s_mixf};
+                      &c.s_mixf, &c.s_eig};
     for (Scratch* s : all) s->buf.reset();
     if (c.stream) cudaStreamSynchronize(c.stream);
-    if (c.solver) cusolverDnDestroy(c.solver);
     if (c.d_info) cudaFree(c.d_info);
+    if (c.d_bar) cudaFree(c.d_bar);
     if (c.d_err) cudaFree(c.d_err);
     if (c.h_pinned) cudaFreeHost(c.h_pinned);
     for (auto& r : c.prof_pending) {
@@ -128,46 +129,18 @@ void Ctx::prof_flush() {
 }
 
 // ---- eigen-decomposition ---------------------------------------------------
-int64_t heevd(Ctx* ctx, cplx* G, int64_t n, double* dlam, int64_t top, bool check) {
-    auto* A = reinterpret_cast<cuDoubleComplex*>(G);
-    const bool partial = top > 0 && top < n;
-    int lwork = 0, meig = (int)n;
-    // top eigenpairs only: the tridiagonal reduction is shared, the
-    // back-transformation covers top columns instead of n
-    const int il = (int)(n - top + 1), iu = (int)n;
-    if (partial)
-        TN_CHECK_SOLVER(cusolverDnZheevdx_bufferSize(
-            ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
-            (int)n, A, (int)n, 0.0, 0.0, il, iu, &meig, dlam, &lwork));
-    else
-        TN_CHECK_SOLVER(cusolverDnZheevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                                    CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n,
-                                                    dlam, &lwork));
-    cuDoubleComplex* work = static_cast<cuDoubleComplex*>(
-        ctx->s_work.get(ctx, sizeof(cuDoubleComplex) * (size_t)std::max(lwork, 1)));
-    ProfScope ps(ctx, 2, 0.0, 16.0 * n * n);
-    if (partial)
-        TN_CHECK_SOLVER(cusolverDnZheevdx(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                          CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, (int)n, A,
-                                          (int)n, 0.0, 0.0, il, iu, &meig, dlam, work, lwork,
-                                          ctx->d_info));
-    else
-        TN_CHECK_SOLVER(cusolverDnZheevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                         CUBLAS_FILL_MODE_LOWER, (int)n, A, (int)n, dlam, work,
-                                         lwork, ctx->d_info));
-    if (check) {
-        int info = 0;
-        TN_CHECK_CUDA(cudaMemcpyAsync(&info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost,
-                                      ctx->stream));
-        ctx->sync();
-        if (info != 0)
-            throw Error(TN_ERR_NUMERIC, std::string(partial ? "zheevdx" : "zheevd") +
-                                            " failed, info = " + std::to_string(info));
+void heev_full(Ctx* ctx, cplx* G, int64_t n, double* dlam) {
+    DBuf V(ctx, sizeof(cplx) * n * n);
+    eig_top(ctx, G, n, n, dlam, V.c());
+    take_top_eigvecs(ctx, V.c(), n, n, G);  // descending -> ascending columns
+    int h = 0;
+    TN_CHECK_CUDA(cudaMemcpyAsync(&h, ctx->d_bar + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    ctx->sync();
+    if (h) {
+        TN_CHECK_CUDA(cudaMemsetAsync(ctx->d_bar + 2, 0, sizeof(unsigned), ctx->stream));
+        throw Error(TN_ERR_TIMEOUT, "eigensolver: a bounded grid barrier ran out");
     }
-    if (partial && meig != (int)top)
-        throw Error(TN_ERR_NUMERIC, "zheevdx returned " + std::to_string(meig) + " of " +
-                                        std::to_string(top) + " eigenpairs");
-    return partial ? top : n;
 }
 
 // ---- truncated split -------------------------------------------------------
@@ -177,10 +150,8 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
     TN_REQUIRE(m > 0 && n > 0, "trunc_split: empty matrix");
     const int64_t sz = std::min(m, n);
     const int64_t g = left_iso ? m : n;
-    TN_REQUIRE(g <= 46340, "trunc_split: Gram matrix too large for 32-bit solver indexing");
+    TN_REQUIRE(g <= 4096, "trunc_split: Gram matrix order above 4096 (bond dimension x d)");
     cplx* G = ctx->s_gram.c(ctx, (size_t)g * g);
-    double* lam = ctx->s_eigval.d(ctx, (size_t)g + sz + 1);
-    double* dS = lam + g;
     const cplx one = cmk(1, 0), zero = cmk(0, 0);
     if (left_iso)  // G = theta theta^H
         zgemm(ctx, OP_N, OP_C, m, m, n, one, theta, m, 0, theta, m, 0, zero, G, m, 0, 1, true);
@@ -189,39 +160,36 @@ SplitResult trunc_split(Ctx* ctx, const cplx* theta, int64_t m, int64_t n, doubl
     // eigenpairs the keep rule can select: max(maxdim, mindim), at most sz
     const int64_t maxd = (maxdim <= 0 || maxdim > sz) ? sz : maxdim;
     const int64_t want = std::min(sz, std::max(maxd, mindim));
-    const bool partial = g >= 32 && want < g;
-    double* dtotal = nullptr;
-    if (partial) {  // the trace gives the weight below the computed eigenvalues
-        dtotal = lam + g + sz;
-        gram_trace(ctx, G, g, dtotal);
-    }
-    // the solver status is read back with the keep-rule result (one synchronisation)
-    const int64_t ne = heevd(ctx, G, g, lam, partial ? want : 0, false);
-    KeepResult kr = keep_rule(ctx, lam, ne, std::min(sz, ne), cutoff, maxdim, mindim, dS, dtotal,
-                              ctx->d_info);
+    double* lam = ctx->s_eigval.d(ctx, (size_t)want + sz + 2);
+    double* dS = lam + want;
+    double* dtotal = lam + want + sz;  // the trace gives the weight below the computed values
+    gram_trace(ctx, G, g, dtotal);
+    cplx* V = ctx->s_x.c(ctx, (size_t)g * want);  // top eigenvectors, descending
+    eig_top(ctx, G, g, want, lam, V);
+    // the eigensolver's barrier status is read back with the keep-rule result
+    KeepResult kr = keep_rule(ctx, lam, want, want, cutoff, maxdim, mindim, dS, dtotal,
+                              reinterpret_cast<const int*>(ctx->d_bar + 2));
     const int64_t k = kr.k;
-    TN_REQUIRE(k <= ne, "trunc_split: keep rule selected more vectors than computed");
+    TN_REQUIRE(k <= want, "trunc_split: keep rule selected more vectors than computed");
     // tensor-core projection in mixed mode, for products large enough to pay
     // for the operand conversion
     const bool use_tc = ctx->mixed && (double)m * n * k >= (double)(1 << 21);
     if (left_iso) {
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
-        take_top_eigvecs(ctx, G, m, k, X.c(), ne);
+        zcopy(ctx, X.c(), V, m * k);
         if (use_tc)  // the isometry stays exact; the projection on the tensor cores
             mixed_gemm(ctx, k, n, m, X.c(), true, theta, Y.c());
         else
             zgemm(ctx, OP_C, OP_N, k, n, m, one, X.c(), m, 0, theta, m, 0, zero, Y.c(), k, 0);
     } else {
-        DBuf V(ctx, sizeof(cplx) * n * k);
-        take_top_eigvecs(ctx, G, n, k, V.c(), ne);
         X = DBuf(ctx, sizeof(cplx) * m * k);
         Y = DBuf(ctx, sizeof(cplx) * k * n);
         if (use_tc)
-            mixed_gemm(ctx, m, k, n, theta, false, V.c(), X.c());
+            mixed_gemm(ctx, m, k, n, theta, false, V, X.c());
         else
-            zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V.c(), n, 0, zero, X.c(), m, 0);
-        conj_transpose(ctx, V.c(), n, k, Y.c());  // Y = V^H (k x n)
+            zgemm(ctx, OP_N, OP_N, m, k, n, one, theta, m, 0, V, n, 0, zero, X.c(), m, 0);
+        conj_transpose(ctx, V, n, k, Y.c());  // Y = V^H (k x n)
     }
     if (S) {
         // Singular values as norms of the projected factor (U^H theta rows or

@@ -1,27 +1,33 @@
 // Two-site effective-Hamiltonian product that allocates nothing.
 //
-// Some callers cannot call cudaMalloc: host programs that run the library
-// inside a device-memory budget they manage themselves (they hand over
-// buffers carved from their own arena and forbid allocations by libraries),
-// and loops where the implicit device synchronisation of an allocation is
-// not acceptable.  For them this entry point takes device pointers for all
+// Some callers cannot call cudaMalloc.  A host that owns the device memory
+// itself (a Julia or C++ program with its own arena and a fixed memory
+// budget) hands the library buffers carved from that arena and does not let
+// a library allocate behind its back; a long-running loop must not fail with
+// an out-of-memory error halfway through a run because another process
+// took the memory.  For them this entry point takes device pointers for all
 // inputs and the output and keeps its intermediates (the L*theta product,
 // the W12-leg product and the merged two-site MPO operator) in one
-// file-scope static device array of fixed size.
+// file-scope static device array of fixed size, reserved when the library is
+// loaded onto a GPU.
 //
 // Limits and sharing:
 //  * the array holds TN_NOALLOC_SCRATCH_BYTES (64 MiB) on every GPU that loads
 //    this library, until the process exits;
 //  * intermediates must fit it: 16*chil*chir*d^2*(wl+wr) + 16*(wl*d^2)*(d^2*wr)
-//    bytes (plus alignment padding); larger problems are rejected;
+//    bytes (plus alignment padding), and the merged operator may have at most
+//    4096 entries (it is staged whole in 64 KiB of shared memory); larger
+//    problems are rejected with TN_ERR_INVALID before anything runs;
 //  * every call uses the same array, which keeps the previous call's
 //    contents; nothing in it needs to start at zero because every
 //    intermediate is fully overwritten before it is read;
 //  * calls whose GPU work overlaps (several streams, threads or contexts at
 //    once) race on the array and must be serialised by the caller;
+//  * like every entry point of the library, a call returns after its work has
+//    finished on the context's stream;
 //  * the first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress, with the context's device made current; make that
+//    first call before any stream capture.
 #include <mutex>
 
 #include "mps.cuh"
@@ -53,11 +59,16 @@ __global__ void w12_kernel(const cplx* __restrict__ W1, const cplx* __restrict__
 std::mutex g_addr_mu;
 void* g_addr[64] = {nullptr};
 
-// Device address of the static array on the current device; resolved once.
+// Device address of the static array on `device`, resolved once per device
+// with that device current (the symbol names a different allocation on
+// every GPU that loaded the library).
 void* scratch_address(int device) {
     TN_REQUIRE(device >= 0 && device < 64, "device index out of range");
     std::lock_guard<std::mutex> lk(g_addr_mu);
     if (!g_addr[device]) {
+        int cur = -1;
+        TN_CHECK_CUDA(cudaGetDevice(&cur));
+        TN_REQUIRE(cur == device, "the context's device must be current");
         void* p = nullptr;
         TN_CHECK_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
         g_addr[device] = p;
@@ -65,11 +76,15 @@ void* scratch_address(int device) {
     return g_addr[device];
 }
 
-void require_device_pointer(const void* p, const char* what) {
+// Accepts device memory of the context's GPU and managed memory; rejects
+// host memory and other GPUs' memory.
+void require_device_pointer(const void* p, const char* what, int device) {
     cudaPointerAttributes a;
     TN_CHECK_CUDA(cudaPointerGetAttributes(&a, p));
     TN_REQUIRE(a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged,
                std::string(what) + " must be a device pointer");
+    TN_REQUIRE(a.type == cudaMemoryTypeManaged || a.device == device,
+               std::string(what) + " lives on another GPU than the context's");
 }
 
 inline size_t align256(size_t b) { return (b + 255) / 256 * 256; }
@@ -86,10 +101,14 @@ void heff2_noalloc(Ctx* ctx, int64_t cl, int64_t cr, int d, int64_t wl, int64_t 
     const size_t bW = align256(sizeof(cplx) * (size_t)(wl * d2) * (d2 * wr));
     TN_REQUIRE(bT1 + bT2 + bW <= TN_NOALLOC_SCRATCH_BYTES,
                "problem exceeds the 64 MiB static scratch of the allocation-free H_eff entry point");
-    TN_REQUIRE((wl * d2) * (d2 * wr) <= 4096, "MPO bond too large for the operator leg");
+    TN_REQUIRE((wl * d2) * (d2 * wr) <= 4096,
+               "merged two-site operator above 4096 entries (64 KiB of shared memory)");
+    // every launch below goes to the context's stream, and the array's
+    // address is per device: make the context's device current first
+    TN_CHECK_CUDA(cudaSetDevice(ctx->device));
     const void* ptrs[] = {L, W1, W2, R, theta, out};
     const char* names[] = {"L", "W1", "W2", "R", "theta", "out"};
-    for (int i = 0; i < 6; ++i) require_device_pointer(ptrs[i], names[i]);
+    for (int i = 0; i < 6; ++i) require_device_pointer(ptrs[i], names[i], ctx->device);
     unsigned char* base = static_cast<unsigned char*>(scratch_address(ctx->device));
     cplx* T1 = reinterpret_cast<cplx*>(base);
     cplx* T2 = reinterpret_cast<cplx*>(base + bT1);

@@ -176,7 +176,7 @@ int64_t split_full(Ctx* ctx, DBuf&& Min, int64_t m, int64_t n, const Trunc& t, b
         zgemm(ctx, OP_N, OP_C, m, m, n, ONE, M, m, 0, M, m, 0, ZERO, G.c(), m, 0, 1, true);
     else
         zgemm(ctx, OP_C, OP_N, n, n, m, ONE, M, m, 0, M, m, 0, ZERO, G.c(), n, 0, 1, true);
-    heevd(ctx, G.c(), g, lam.d());
+    heev_full(ctx, G.c(), g, lam.d());
     const KeepResult kr = keep_rule(ctx, lam.d(), g, sz, t.cutoff, t.maxdim, t.mindim, nullptr);
     const int64_t k = kr.k;
     X = DBuf(ctx, sizeof(cplx) * m * k);

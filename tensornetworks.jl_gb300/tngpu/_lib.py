@@ -85,6 +85,7 @@ _SIGS = {
     "tn_gate2_apply": (i32, [P, i64, i64, i64, i32, dp, dp, dp, dp]),
     "tn_truncate": (i32, [P, i64, i64, dp, C.POINTER(TruncOpts), i32, dp, dp, dp, i64p]),
     "tn_gemm": (i32, [P, i64, i64, i64, dp, i32, dp, dp, i32]),
+    "tn_eigh_top": (i32, [P, i64, dp, i64, dp, dp]),
     "tn_profile_enable": (i32, [P, i32]),
     "tn_profile_reset": (i32, [P]),
     "tn_profile_read": (i32, [P, i64p, dp, dp, dp]),
