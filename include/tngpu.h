@@ -37,6 +37,12 @@ extern "C" {
 
 #define TN_PREC_FP64   0   /* plain FP64 (parity mode)                          */
 #define TN_PREC_MIXED  1   /* 3xTF32 tcgen05 products, FP64 Lanczos/truncation */
+#define TN_PREC_MIXED_ENV64 2 /* tn_dmrg / tn_dmrg_sum only: as TN_PREC_MIXED for
+                                 the H_eff products and truncation projections,
+                                 with the environment blocks updated in FP64
+                                 (their 3xTF32 rounding otherwise compounds
+                                 along the chain into a ~1e-5 scale error of
+                                 H_eff)                                       */
 
 typedef struct tn_ctx tn_ctx;
 typedef struct tn_mps tn_mps;     /* GMPS of rank 1 on the device */
@@ -153,6 +159,21 @@ int32_t tn_inner_terms(tn_ctx* ctx, const tn_mps* bra, const tn_mps* ket, int32_
 /* ---- DMRG (src/algorithms/mps/dmrg.jl:1-154) ------------------------------ */
 int32_t tn_dmrg(tn_ctx* ctx, tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts* opts,
                 double* energy, tn_dmrg_stats* stats);
+
+/* dmrg(psi, Hs::GMPS...; coeffs) over a sum of terms (dmrg.jl:128-154,
+ * projmpssum.jl:51-108): nmpo MPOs with coefficients mpo_coeffs (NULL: all
+ * 1), each ProjMPS(psi, H, psi; rank=2), and nproj MPS terms with
+ * coefficients proj_coeffs (NULL: all 1), each ProjMPS(phi, psi; rank=2,
+ * squared=true), whose product is coeff |phi><phi|psi> on the two sites
+ * (projmps.jl:103-145) -- the penalty that targets excited states.  The
+ * initial cost is the terms' calculate (a projector contributes coeff
+ * <phi|psi>, as projmps.jl:192-216 does); energy_fp64 in the stats is
+ * sum_t c_t <psi|H_t|psi> + sum_p c_p |<phi_p|psi>|^2 of the final state.
+ * The projector states are read, not modified. */
+int32_t tn_dmrg_sum(tn_ctx* ctx, tn_mps* psi, int32_t nmpo, const tn_mpo* const* mpos,
+                    const double* mpo_coeffs, int32_t nproj, const tn_mps* const* projs,
+                    const double* proj_coeffs, const tn_dmrg_opts* opts, double* energy,
+                    tn_dmrg_stats* stats);
 
 /* ---- gates (structures/mps/gatelist.jl) ----------------------------------- */
 /* nrows rows; row r has row_len[r] gates; sites/gate_nsites/gate_ptrs list all

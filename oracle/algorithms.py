@@ -8,7 +8,7 @@ import math
 import numpy as np
 import scipy.linalg as sla
 
-from .core import (GMPS, OpList, ProjMPS, applyop, fr, inner, siterange,
+from .core import (ProjMPSSum, GMPS, OpList, ProjMPS, applyop, fr, inner, siterange,
                    sitetensor)
 
 __all__ = [
@@ -107,18 +107,28 @@ def lanczos_lowest(matvec, x0, krylovdim, maxiter, tol=1e-14, stats=None):
 # ---------------------------------------------------------------------------
 def dmrg(psi, H, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1, maxsweeps=1000,
          tol=1e-10, tolgrad=1e-5, numconverges=4.0, cutoff=1e-12, maxdim=1000,
-         mindim=1, verbose=False, stats=None, energies=None):
-    """Two-site DMRG (dmrg.jl:1-99 and the MPO entry point dmrg.jl:128-154).
+         mindim=1, verbose=False, stats=None, energies=None, coeffs=None):
+    """Two-site DMRG (dmrg.jl:1-99 and the entry point dmrg.jl:128-154).
 
-    One directional pass is one sweep (dmrg.jl:63-66).  Returns (psi, cost)
-    with cost the last local Lanczos eigenvalue (dmrg.jl:55,98)."""
+    ``H`` is one MPO or a list of terms: MPOs (rank 2, ProjMPS(psi, H, psi))
+    and MPSs (rank 1, ProjMPS(phi, psi; squared=true)), weighted by
+    ``coeffs``, summed in a ProjMPSSum.  One directional pass is one sweep
+    (dmrg.jl:63-66).  Returns (psi, cost) with cost the last local Lanczos
+    eigenvalue (dmrg.jl:55,98)."""
     if nsites != 2:
         raise ValueError("only two-site DMRG is on this path")
     if psi.rank != 1:
         raise ValueError("Psi must be a GMPS of rank 1 (vector).")
     psi.movecenter(1)
     N = len(psi)
-    proj = ProjMPS(psi, psi, H, center=1)
+    if isinstance(H, (list, tuple)):
+        cs = [1.0] * len(H) if coeffs is None else list(coeffs)
+        terms = [ProjMPS(psi, psi, h, center=1, coeff=c) if h.rank == 2
+                 else ProjMPS(h, psi, None, center=1, coeff=c, squared=True)
+                 for h, c in zip(H, cs)]
+        proj = ProjMPSSum(terms, center=1)
+    else:
+        proj = ProjMPS(psi, psi, H, center=1)
     cost = proj.calculate()
     lastcost = cost
     D = psi.maxbonddim()

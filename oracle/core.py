@@ -549,8 +549,9 @@ class ProjMPS:
     the left block through site i when i < centre, or the right block from
     site i when i > centre."""
 
-    def __init__(self, bra, ket, mpo=None, center=1, coeff=1.0):
+    def __init__(self, bra, ket, mpo=None, center=1, coeff=1.0, squared=False):
         self.bra, self.ket, self.mpo = bra, ket, mpo
+        self.squared = squared
         self.nobj = 2 if mpo is None else 3
         self.blocks = [_edge(self.nobj) for _ in range(len(bra))]
         self.center = 0
@@ -591,11 +592,26 @@ class ProjMPS:
         self.center = idx
 
     def product(self, theta, direction):
-        """projmps.jl:103-145 with nsites=2."""
+        """projmps.jl:103-145 with nsites=2: the MPO branch, or for a squared
+        bra-ket projection coeff * (sum P theta) * conj(P), P = project()."""
+        if self.mpo is None:
+            P = self.project(direction)
+            s = np.sum(P * theta)
+            fac = np.conj(P) if self.squared else 1.0
+            return s * fac * self.coeff
         site = self.center - 1 if direction else self.center
         out = heff2(self.block(site - 1), self.mpo[site], self.mpo[site + 1],
                     self.block(site + 2), theta)
         return out * self.coeff
+
+    def project(self, direction):
+        """projmps.jl:156-189 (no MPO, nsites=2): the bra's two sites
+        contracted with the overlap blocks, P[b,s1,s2,c] = sum L[x,b]
+        conj(bra1[x,s1,y]) conj(bra2[y,s2,z]) R[z,c]."""
+        site = self.center - 1 if direction else self.center
+        L, R = self.block(site - 1), self.block(site + 2)
+        B1, B2 = np.conj(self.bra[site]), np.conj(self.bra[site + 1])
+        return np.einsum("xb,xsy,ytz,zc->bstc", L, B1, B2, R, optimize=True)
 
     def calculate(self):
         """Full contraction at the centre (projmps.jl:192-216)."""
@@ -603,6 +619,30 @@ class ProjMPS:
         left = env_left(self.block(site - 1), self.bra[site], self._W(site), self.ket[site])
         right = self.block(site + 1)
         return self.coeff * np.sum(left * right)
+
+
+class ProjMPSSum:
+    """A sum of projections (projmpssum.jl:1-108): movecenter, product and
+    calculate add the terms'."""
+
+    def __init__(self, projs, center=1):
+        self.projs = list(projs)
+        self.center = 0
+        self.movecenter(center)
+
+    def movecenter(self, idx):
+        for p in self.projs:
+            p.movecenter(idx)
+        self.center = idx
+
+    def product(self, theta, direction):
+        out = self.projs[0].product(theta, direction)
+        for p in self.projs[1:]:
+            out = out + p.product(theta, direction)
+        return out
+
+    def calculate(self):
+        return sum(p.calculate() for p in self.projs)
 
 
 def inner(st, psi, oplist, phi):

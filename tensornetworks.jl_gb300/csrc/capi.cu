@@ -7,8 +7,6 @@
 #include "mps.cuh"
 
 namespace tn {
-void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energy,
-              tn_dmrg_stats* stats);
 void applygates(tn_mps* psi, const tn_gates* g, const Trunc& t);
 void tebd_steps(tn_mps* psi, const tn_gates* g, int nsteps, const Trunc& t, double* lognorm);
 std::vector<double> qjmc_rates(tn_mps* psi, const std::vector<DBuf>& LdL,
@@ -423,7 +421,32 @@ int32_t tn_dmrg(tn_ctx* h, tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts* opt
                 tn_dmrg_stats* stats) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(psi && H && opts && energy, "null argument");
-    dmrg_run(psi, H, *opts, energy, stats);
+    DmrgTerms terms;
+    terms.H.push_back(H);
+    terms.hc.push_back(1.0);
+    dmrg_run(psi, terms, *opts, energy, stats);
+    TN_API_END
+}
+
+int32_t tn_dmrg_sum(tn_ctx* h, tn_mps* psi, int32_t nmpo, const tn_mpo* const* mpos,
+                    const double* mpo_coeffs, int32_t nproj, const tn_mps* const* projs,
+                    const double* proj_coeffs, const tn_dmrg_opts* opts, double* energy,
+                    tn_dmrg_stats* stats) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(psi && opts && energy && nmpo >= 0 && nproj >= 0, "null argument");
+    TN_REQUIRE(nmpo == 0 || mpos, "null MPO list");
+    TN_REQUIRE(nproj == 0 || projs, "null projector list");
+    DmrgTerms terms;
+    for (int t = 0; t < nmpo; ++t) {
+        terms.H.push_back(mpos[t]);
+        terms.hc.push_back(mpo_coeffs ? mpo_coeffs[t] : 1.0);
+    }
+    for (int p = 0; p < nproj; ++p) {
+        TN_REQUIRE(projs[p] != psi, "a projector term must not be the optimised state");
+        terms.P.push_back(projs[p]);
+        terms.pc.push_back(proj_coeffs ? proj_coeffs[p] : 1.0);
+    }
+    dmrg_run(psi, terms, *opts, energy, stats);
     TN_API_END
 }
 

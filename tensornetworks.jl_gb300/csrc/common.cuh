@@ -179,6 +179,7 @@ void multi_dot(Ctx* ctx, const cplx* const* dV, int K, const cplx* w, int64_t n,
 void multi_axpy(Ctx* ctx, cplx* w, const cplx* const* dV, const cplx* dcoef, int K, int64_t n,
                 double sign);
 void zscale(Ctx* ctx, cplx* x, int64_t n, cplx a);
+void zaxpy(Ctx* ctx, cplx* y, const cplx* x, int64_t n, cplx a);  // y += a x
 void zscale_dev(Ctx* ctx, cplx* x, int64_t n, const double* dnorm, int invert);  // x *= 1/norm
 void zcopy(Ctx* ctx, cplx* dst, const cplx* src, int64_t n);
 void zfill(Ctx* ctx, cplx* dst, int64_t n, cplx v);

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include "mixed.cuh"
 #include "mps.cuh"
@@ -194,6 +195,7 @@ struct EnvCache {
     std::vector<int64_t> a, w, b;
     DBuf edge;
     int center = 0;
+    bool env_mixed = true;  // with ctx->mixed: 3xTF32 environment updates
     EnvCache(tn_mps* p, const tn_mpo* h) : ctx(p->ctx), psi(p), H(h), N(p->N) {
         blk.resize(N + 2);
         a.assign(N + 2, 1);
@@ -217,7 +219,7 @@ struct EnvCache {
         const cplx* L = block(i - 1, la, lw, lb);
         const int64_t na = psi->dr(i), nw = H->w[i], nb = psi->dr(i);
         DBuf out(ctx, sizeof(cplx) * na * nw * nb);
-        if (ctx->mixed)
+        if (ctx->mixed && env_mixed)
             mixed_env_left(ctx, L, la, lw, lb, psi->site(i), na, H->Ml[i - 1].c(), psi->d, nw,
                            psi->site(i), nb, out.c());
         else
@@ -232,7 +234,7 @@ struct EnvCache {
         const cplx* R = block(i + 1, ra, rw, rb);
         const int64_t na = psi->dl(i), nw = H->w[i - 1], nb = psi->dl(i);
         DBuf out(ctx, sizeof(cplx) * na * nw * nb);
-        if (ctx->mixed)
+        if (ctx->mixed && env_mixed)
             mixed_env_right(ctx, R, ra, rw, rb, psi->site(i), na, H->Mr[i - 1].c(), psi->d, nw,
                             psi->site(i), nb, out.c());
         else
@@ -270,15 +272,119 @@ struct EnvCache {
     }
 };
 
-void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energy,
+// ---- overlap cache <phi|psi> of a projector term (ProjMPS(phi, psi;
+// squared=true), projmps.jl:16-95 with the objects [phi, psi]) --------------------
+struct OvlCache {
+    Ctx* ctx;
+    const tn_mps* phi;
+    tn_mps* psi;
+    int N;
+    std::vector<DBuf> blk;  // blk[i]: left block through i (i < centre) or right block from i
+    std::vector<int64_t> a, b;
+    DBuf edge;
+    int center = 0;
+    OvlCache(const tn_mps* f, tn_mps* p) : ctx(p->ctx), phi(f), psi(p), N(p->N) {
+        blk.resize(N + 2);
+        a.assign(N + 2, 1);
+        b.assign(N + 2, 1);
+        edge = DBuf(ctx, sizeof(cplx));
+        zfill(ctx, edge.c(), 1, ONE);
+    }
+    const cplx* block(int i, int64_t& ca, int64_t& cb) const {
+        if (i < 1 || i > N) {
+            ca = cb = 1;
+            return edge.c();
+        }
+        ca = a[i];
+        cb = b[i];
+        return blk[i].c();
+    }
+    void buildleft(int i) {
+        int64_t la, lb;
+        const cplx* L = block(i - 1, la, lb);
+        const int64_t na = phi->dr(i), nb = psi->dr(i);
+        DBuf out(ctx, sizeof(cplx) * na * nb);
+        env_left(ctx, L, la, 1, lb, phi->site(i), na, nullptr, i, psi->site(i), nb, psi->d, out.c());
+        blk[i] = std::move(out);
+        a[i] = na;
+        b[i] = nb;
+    }
+    void buildright(int i) {
+        int64_t ra, rb;
+        const cplx* R = block(i + 1, ra, rb);
+        const int64_t na = phi->dl(i), nb = psi->dl(i);
+        DBuf out(ctx, sizeof(cplx) * na * nb);
+        env_right(ctx, R, ra, 1, rb, phi->site(i), na, nullptr, i, psi->site(i), nb, psi->d, out.c());
+        blk[i] = std::move(out);
+        a[i] = na;
+        b[i] = nb;
+    }
+    void movecenter(int idx) {  // abstractprojmps.jl:60-81
+        if (center == 0) {
+            for (int i = 1; i <= idx - 1; ++i) buildleft(i);
+            for (int i = 1; i <= N - idx; ++i) buildright(N + 1 - i);
+        } else if (idx > center) {
+            for (int i = 1; i <= idx - center; ++i) buildleft(center - 1 + i);
+        } else if (idx < center) {
+            for (int i = 1; i <= center - idx; ++i) buildright(center + 1 - i);
+        }
+        center = idx;
+    }
+    // <phi|psi> contracted at the centre (calculate, projmps.jl:192-216)
+    cplx calculate() {
+        const int c = center;
+        int64_t la, lb, ra, rb;
+        const cplx* L = block(c - 1, la, lb);
+        const cplx* R = block(c + 1, ra, rb);
+        const int64_t na = phi->dr(c), nb = psi->dr(c);
+        DBuf out(ctx, sizeof(cplx) * na * nb);
+        env_left(ctx, L, la, 1, lb, phi->site(c), na, nullptr, c, psi->site(c), nb, psi->d, out.c());
+        cplx* d = ctx->s_coef.c(ctx, 4);
+        bilinear_dot(ctx, out.c(), R, na * nb, d);
+        cplx hres;
+        TN_CHECK_CUDA(cudaMemcpyAsync(&hres, d, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->sync();
+        return hres;
+    }
+    // The projected two-site ket of phi in psi's local basis at bond
+    // (site1, site1+1): K[b, s1, s2, c] = sum conj(L[x, b]) phi1[x, s1, y]
+    // phi2[y, s2, z] conj(R[z, c]), i.e. conj of project() (projmps.jl:156-189).
+    void local_ket(int site1, DBuf& K) {
+        const int d = psi->d;
+        int64_t la, lb, ra, rb;
+        const cplx* L = block(site1 - 1, la, lb);
+        const cplx* R = block(site1 + 2, ra, rb);
+        const int64_t x = phi->dl(site1), y = phi->dr(site1), z = phi->dr(site1 + 1);
+        DBuf Phi(ctx, sizeof(cplx) * x * d * d * z), T(ctx, sizeof(cplx) * lb * d * d * z);
+        zgemm(ctx, OP_N, OP_N, x * d, d * z, y, ONE, phi->site(site1), x * d, 0, phi->site(site1 + 1),
+              y, 0, cmk(0, 0), Phi.c(), x * d, 0);
+        zgemm(ctx, OP_C, OP_N, lb, d * d * z, la, ONE, L, la, 0, Phi.c(), x, 0, cmk(0, 0), T.c(), lb, 0);
+        const size_t nk = sizeof(cplx) * lb * d * d * rb;
+        if (K.bytes < nk) K = DBuf(ctx, nk);
+        zgemm(ctx, OP_N, OP_R, lb * d * d, rb, z, ONE, T.c(), lb * d * d, 0, R, ra, 0, cmk(0, 0), K.c(),
+              lb * d * d, 0);
+    }
+};
+
+void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double* energy,
               tn_dmrg_stats* stats) {
     Ctx* ctx = psi->ctx;
     const int N = psi->N, d = psi->d;
     TN_REQUIRE(o.nsites == 2, "only two-site DMRG (nsites=2) is on this path");
-    TN_REQUIRE(H->N == N, "GMPS must share the same properties.");
-    TN_REQUIRE(H->d == d, "GMPS must share the same properties.");
+    TN_REQUIRE(!terms.H.empty() || !terms.P.empty(),
+               "You must provide atleast one MPS/MPO for the Hamiltonian.");
+    TN_REQUIRE(terms.hc.size() == terms.H.size() && terms.pc.size() == terms.P.size(),
+               "one coefficient per term");
+    for (const tn_mpo* H : terms.H)
+        TN_REQUIRE(H && H->N == N && H->d == d, "GMPS must share the same properties.");
+    for (const tn_mps* P : terms.P)
+        TN_REQUIRE(P && P->N == N && P->d == d, "GMPS must share the same properties.");
+    const size_t nh = terms.H.size(), np = terms.P.size();
     TN_REQUIRE(N >= 2, "DMRG needs at least two sites");
-    TN_REQUIRE(o.precision == TN_PREC_FP64 || o.precision == TN_PREC_MIXED, "unknown precision");
+    TN_REQUIRE(o.precision == TN_PREC_FP64 || o.precision == TN_PREC_MIXED ||
+                   o.precision == TN_PREC_MIXED_ENV64,
+               "unknown precision");
+    const bool mixed_heff = o.precision != TN_PREC_FP64;
     auto t0 = std::chrono::steady_clock::now();
     // mixed precision: environment updates and truncation projections run on
     // the tensor cores for the whole call; restored on every exit path
@@ -287,11 +393,31 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         bool old;
         ~MixedMode() { c->mixed = old; }
     } mode_guard{ctx, ctx->mixed};
-    ctx->mixed = (o.precision == TN_PREC_MIXED);
+    // ctx->mixed: H_eff products and truncation projections on the tensor
+    // cores; the environment updates follow EnvCache::env_mixed (FP64 with
+    // TN_PREC_MIXED_ENV64)
+    ctx->mixed = mixed_heff;
     movecenter(psi, 1, no_trunc());
-    EnvCache env(psi, H);
-    env.movecenter(1);
-    cplx cost = env.calculate();
+    std::vector<std::unique_ptr<EnvCache>> envs;
+    std::vector<std::unique_ptr<OvlCache>> ovls;
+    for (const tn_mpo* H : terms.H) {
+        envs.emplace_back(new EnvCache(psi, H));
+        envs.back()->env_mixed = o.precision == TN_PREC_MIXED;
+    }
+    for (const tn_mps* P : terms.P) ovls.emplace_back(new OvlCache(P, psi));
+    // initial cost: the sum of the terms' calculate (projmpssum.jl:101-108);
+    // a projector term contributes coeff <phi|psi> as ProjMPS's calculate does
+    cplx cost = cmk(0, 0);
+    for (size_t t = 0; t < nh; ++t) {
+        envs[t]->movecenter(1);
+        const cplx v = envs[t]->calculate();
+        cost = cadd(cost, cmk(terms.hc[t] * v.x, terms.hc[t] * v.y));
+    }
+    for (size_t p = 0; p < np; ++p) {
+        ovls[p]->movecenter(1);
+        const cplx v = ovls[p]->calculate();
+        cost = cadd(cost, cmk(terms.pc[p] * v.x, terms.pc[p] * v.y));
+    }
     cplx lastcost = cost;
     int D = psi->maxbonddim(), lastD = D;
     double grad = 0.0;
@@ -300,8 +426,9 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
     int64_t matvecs = 0;
     double last_disc = 0.0;
     const Trunc tr{o.cutoff, o.maxdim, o.mindim};
-    DBuf theta, vec, out;
-    MixedWork mw;
+    DBuf theta, vec, out, tmp;
+    std::vector<MixedWork> mws(nh);
+    std::vector<DBuf> kets(np), kets_c(np);
     int bond_updates = 0;
     bool sample_done = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -336,30 +463,58 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
                 ctx->phase_s[k] += std::chrono::duration<double>(now - tp).count();
                 tp = now;
             };
-            env.movecenter(site);
+            for (auto& e : envs) e->movecenter(site);
+            for (auto& e : ovls) e->movecenter(site);
             phase(0);
             two_site(psi, site1, theta);
             const int64_t cl = psi->dl(site1), cr = psi->dr(site1 + 1);
             const int64_t n = cl * d * d * cr;
-            int64_t la, lw, lb, ra, rw, rb;
-            const cplx* L = env.block(site1 - 1, la, lw, lb);
-            const cplx* R = env.block(site1 + 2, ra, rw, rb);
-            const cplx* W12 = H->W12[site1 - 1].c();
-            MatVec mv;
-            if (o.precision == TN_PREC_MIXED) {
-                mixed_prepare_env(ctx, mw, L, R, cl, cr, d, lw, rw);
-                mv = [&, cl, cr, lw, rw, W12](const cplx* x, cplx* y) {
-                    mixed_heff2(ctx, mw, W12, cl, cr, d, lw, rw, x, y);
-                };
-            } else {
-                mv = [&, L, R, cl, cr, lw, rw, W12](const cplx* x, cplx* y) {
-                    heff2_fp64(ctx, L, W12, R, cl, cr, d, lw, rw, x, y);
-                };
+            // per MPO term: environment blocks (and mixed-precision operand planes)
+            std::vector<const cplx*> Ls(nh), Rs(nh);
+            std::vector<int64_t> lws(nh), rws(nh);
+            for (size_t t = 0; t < nh; ++t) {
+                int64_t la, lb, ra, rb;
+                Ls[t] = envs[t]->block(site1 - 1, la, lws[t], lb);
+                Rs[t] = envs[t]->block(site1 + 2, ra, rws[t], rb);
+                if (mixed_heff)
+                    mixed_prepare_env(ctx, mws[t], Ls[t], Rs[t], cl, cr, d, lws[t], rws[t]);
             }
+            // per projector term: the local ket K and coeff * K
+            for (size_t p = 0; p < np; ++p) {
+                ovls[p]->local_ket(site1, kets[p]);
+                if (kets_c[p].bytes < sizeof(cplx) * n) kets_c[p] = DBuf(ctx, sizeof(cplx) * n);
+                zcopy(ctx, kets_c[p].c(), kets[p].c(), n);
+                zscale(ctx, kets_c[p].c(), n, cmk(terms.pc[p], 0.0));
+            }
+            if (nh > 1 && tmp.bytes < sizeof(cplx) * n) tmp = DBuf(ctx, sizeof(cplx) * n);
+            cplx* dproj = ctx->s_mixf.c(ctx, std::max<size_t>(np, 1));
+            // y = sum_t c_t H_t x + sum_p c_p K_p <K_p|x>  (product, projmpssum.jl:74-86)
+            MatVec mv = [&, cl, cr, site1](const cplx* x, cplx* y) {
+                for (size_t t = 0; t < nh; ++t) {
+                    cplx* dst = (t == 0) ? y : tmp.c();
+                    const cplx* W12 = terms.H[t]->W12[site1 - 1].c();
+                    if (mixed_heff)
+                        mixed_heff2(ctx, mws[t], W12, cl, cr, d, lws[t], rws[t], x, dst);
+                    else
+                        heff2_fp64(ctx, Ls[t], W12, Rs[t], cl, cr, d, lws[t], rws[t], x, dst);
+                    if (t == 0) {
+                        if (terms.hc[0] != 1.0) zscale(ctx, y, n, cmk(terms.hc[0], 0.0));
+                    } else {
+                        zaxpy(ctx, y, tmp.c(), n, cmk(terms.hc[t], 0.0));
+                    }
+                }
+                if (nh == 0) zfill(ctx, y, n, cmk(0, 0));
+                for (size_t p = 0; p < np; ++p) {
+                    const cplx* kp = kets[p].c();
+                    const cplx* kc = kets_c[p].c();
+                    multi_dot(ctx, &kp, 1, x, n, dproj + p);
+                    multi_axpy(ctx, y, &kc, dproj + p, 1, n, 1.0);
+                }
+            };
             phase(1);
             LanczosOut lo = lanczos_lowest(ctx, n, theta.c(), mv, o.krylovdim, o.kryloviter, 1e-14, vec);
             matvecs += lo.numops;
-            if (o.precision == TN_PREC_MIXED) tc_check_error(ctx);
+            if (mixed_heff) tc_check_error(ctx);
             phase(2);
             cost = cmk(lo.eig, 0.0);
             SplitResult sr = replacesites2(psi, vec.c(), site1, direction, true, tr);
@@ -374,7 +529,8 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
             ++bond_updates;
         }
         if (sample_done) break;
-        env.movecenter(direction ? 1 : N);
+        for (auto& e : envs) e->movecenter(direction ? 1 : N);
+        for (auto& e : ovls) e->movecenter(direction ? 1 : N);
         TN_CHECK_CUDA(cudaEventRecord(ev1, ctx->stream));
         TN_CHECK_CUDA(cudaEventSynchronize(ev1));
         float ms = 0.f;
@@ -410,23 +566,35 @@ void dmrg_run(tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts& o, double* energ
         ctx->prof_on = false;
     }
     double e64 = cost.x;
-    if (o.precision == TN_PREC_FP64 && !sample_done) {
-        // <psi|H|psi> of the final state (the returned cost is the last local
-        // Lanczos eigenvalue, as in dmrg.jl:55,98)
-        env.movecenter(psi->center);
-        e64 = env.calculate().x;
-    } else if (o.precision == TN_PREC_MIXED && !sample_done) {
-        // FP64 recomputation of the energy: <psi|H|psi> from environments
-        // rebuilt in FP64 (the sweep's own blocks carry 3xTF32 rounding)
+    if (!sample_done) {
+        // <psi|H|psi> of the final state: sum_t c_t <psi|H_t|psi> + sum_p c_p
+        // |<phi_p|psi>|^2 (the returned cost is the last local Lanczos
+        // eigenvalue, as in dmrg.jl:55,98); with 3xTF32 environments it comes
+        // from environments rebuilt in FP64
+        const bool rebuild = o.precision == TN_PREC_MIXED;
         ctx->mixed = false;
-        EnvCache env64(psi, H);
-        env64.movecenter(psi->center);
-        e64 = env64.calculate().x;
+        double acc = 0.0;
+        for (size_t t = 0; t < nh; ++t) {
+            if (rebuild) {
+                EnvCache env64(psi, terms.H[t]);
+                env64.movecenter(psi->center);
+                acc += terms.hc[t] * env64.calculate().x;
+            } else {
+                envs[t]->movecenter(psi->center);
+                acc += terms.hc[t] * envs[t]->calculate().x;
+            }
+        }
+        for (size_t p = 0; p < np; ++p) {
+            ovls[p]->movecenter(psi->center);
+            const cplx v = ovls[p]->calculate();
+            acc += terms.pc[p] * (v.x * v.x + v.y * v.y);
+        }
+        e64 = acc;
     }
     // FP64 mode returns the last local eigenvalue as the reference does; mixed
     // mode returns the FP64 <psi|H|psi> (its Lanczos values carry the
     // tensor-core accumulation bias of the environments, ~1e-5 relative)
-    *energy = (o.precision == TN_PREC_MIXED && !sample_done) ? e64 : cost.x;
+    *energy = (mixed_heff && !sample_done) ? e64 : cost.x;
     if (stats) {
         stats->sweeps = sweeps;
         stats->maxbonddim = D;

@@ -297,6 +297,12 @@ __global__ void multi_axpy_kernel(cplx* __restrict__ w, PtrPack V, const cplx* _
     }
 }
 
+__global__ void zaxpy_kernel(cplx* __restrict__ y, const cplx* __restrict__ x, int64_t n, cplx a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = cfma(a, x[i], y[i]);
+}
+
 __global__ void zscale_kernel(cplx* x, int64_t n, cplx a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -611,6 +617,14 @@ void multi_axpy(Ctx* ctx, cplx* w, const cplx* const* hV, const cplx* dcoef, int
         }
         ctx->count();
     }
+    TN_CHECK_CUDA(cudaGetLastError());
+}
+
+void zaxpy(Ctx* ctx, cplx* y, const cplx* x, int64_t n, cplx a) {
+    if (n <= 0) return;
+    ProfScope ps(ctx, 6, 8.0 * n, 48.0 * n);
+    zaxpy_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(y, x, n, a);
+    ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
 }
 

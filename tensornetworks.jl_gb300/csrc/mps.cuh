@@ -92,6 +92,18 @@ struct Term {
 std::vector<cplx> inner_terms(Ctx* ctx, const tn_mps* bra, const tn_mps* ket,
                               const std::vector<Term>& terms);
 
+// Terms of dmrg(psi, Hs::GMPS...; coeffs) (dmrg.jl:128-154, projmpssum.jl):
+// MPOs H[t] with coefficients hc[t] (ProjMPS(psi, H, psi; rank=2)) and MPS
+// projectors coeff pc[p] |P[p]><P[p]| (ProjMPS(P, psi; rank=2, squared=true)).
+struct DmrgTerms {
+    std::vector<const tn_mpo*> H;
+    std::vector<double> hc;
+    std::vector<const tn_mps*> P;
+    std::vector<double> pc;
+};
+void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double* energy,
+              tn_dmrg_stats* stats);
+
 // TEBD adjoint (tebd_grad.cu): f = <O at obs_site> after the steps (step s
 // applies gate list gls[step_gl[s]] then normalises); grads != null receives
 // df/dconj(G) for every gate of every list in the upload layouts

@@ -18,7 +18,7 @@ LIBPATH = os.path.join(HERE, "libtngpu.so")
 TN_OK = 0
 TN_ERR = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "device wait timed out", -5: "numerical failure"}
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "mixed-env64": 2}
 
 i32, i64, f64 = C.c_int32, C.c_int64, C.c_double
 P = C.c_void_p
@@ -66,6 +66,8 @@ _SIGS = {
     "tn_mps_applyop": (i32, [P, P, i32, dp]),
     "tn_inner_terms": (i32, [P, P, P, i32, i32p, i32p, dp, dp, dp]),
     "tn_dmrg": (i32, [P, P, P, C.POINTER(DmrgOpts), dp, C.POINTER(DmrgStats)]),
+    "tn_dmrg_sum": (i32, [P, P, i32, C.POINTER(P), dp, i32, C.POINTER(P), dp,
+                          C.POINTER(DmrgOpts), dp, C.POINTER(DmrgStats)]),
     "tn_gates_upload": (i32, [P, i32, i32, i32, i32p, i32p, i32p, dpp, C.POINTER(P)]),
     "tn_gates_destroy": (i32, [P]),
     "tn_applygates": (i32, [P, P, P, C.POINTER(TruncOpts)]),
@@ -92,7 +94,7 @@ _SIGS = {
     "tn_profile_phases": (i32, [P, dp]),
 }
 
-PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "zheevd/zheevdx (cuSOLVER FP64)",
+PROF_CLASSES = ("tc_cgemm_kernel (tcgen05 3xTF32)", "zgemm_kernel (FP64)", "eigensolver (own FP64: tridiagonal, bisection, inverse iteration, QR, back-transform)",
                 "small_apply_kernel (FP64 legs)", "heff_mid_kernel (FP32 leg)",
                 "operand conversion / partial reduction", "Lanczos vector ops",
                 "all launches (count only)")

@@ -21,19 +21,32 @@ from .mps import GMPS, MPOHandle, inner
 # ---------------------------------------------------------------------------
 # DMRG (dmrg.jl:1-154)
 # ---------------------------------------------------------------------------
-def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
+def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
          maxsweeps=1000, tol=1e-10, tolgrad=1e-5, numconverges=4, cutoff=1e-12, maxdim=1000,
          mindim=1, verbose=True, precision="fp64", stats=None, max_bond_updates=0,
-         profile_from_sweep=-1):
+         profile_from_sweep=-1, coeffs=None):
     """Two-site DMRG; mutates ``psi`` and returns (psi, energy).
 
-    ``stats`` (a dict) receives sweeps, matvecs, per-sweep device seconds and
-    energies; ``max_bond_updates`` > 0 stops after that many bond
-    optimisations (a bounded timing sample)."""
+    ``Hs`` are the terms of dmrg(psi, Hs::GMPS...; coeffs) (dmrg.jl:128-154):
+    MPOs (rank 2) and MPSs (rank 1, each the penalty coeff |phi><phi|, as
+    ProjMPS(phi, psi; squared=true) gives), weighted by ``coeffs`` (default
+    all 1).  ``precision``: "fp64", "mixed" (3xTF32 tensor-core H_eff,
+    environments and projections) or "mixed-env64" (the same with FP64
+    environment updates).  ``stats`` (a dict) receives sweeps, matvecs,
+    per-sweep device seconds and energies; ``max_bond_updates`` > 0 stops
+    after that many bond optimisations (a bounded timing sample)."""
     if psi.rank != 1:
         raise ValueError("Psi must be a GMPS of rank 1 (vector).")
-    if len(H) != len(psi) or H.dim != psi.dim:
-        raise ValueError("GMPS must share the same properties.")
+    if len(Hs) == 0:
+        raise ValueError("You must provide atleast one MPS/MPO for the Hamiltonian.")
+    coeffs = [1.0] * len(Hs) if coeffs is None else [float(c) for c in coeffs]
+    if len(coeffs) != len(Hs):
+        raise ValueError("one coefficient per Hamiltonian term")
+    for H in Hs:
+        if len(H) != len(psi) or H.dim != psi.dim:
+            raise ValueError("GMPS must share the same properties.")
+        if H.rank not in (1, 2):
+            raise ValueError("Hamiltonian must be composed of MPOs (rank 2) or MPSs (rank 1).")
     if nsites != 2:
         raise ValueError("only two-site DMRG (nsites=2) is on this path")
     o = L.DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
@@ -53,7 +66,17 @@ def dmrg(psi: GMPS, H: MPOHandle, nsites=2, krylovdim=3, kryloviter=2, minsweeps
     st.bond_cap = bcap
     st.bond_seconds, st.bond_chi = L.as_dp(bsec), bchi.ctypes.data_as(L.i32p)
     ctx = psi.ctx
-    ctx.check(ctx.lib.tn_dmrg(ctx.h, psi._h, H._h, C.byref(o), C.byref(e), C.byref(st)))
+    if len(Hs) == 1 and Hs[0].rank == 2 and coeffs[0] == 1.0:
+        ctx.check(ctx.lib.tn_dmrg(ctx.h, psi._h, Hs[0]._h, C.byref(o), C.byref(e), C.byref(st)))
+    else:
+        mpos = [H for H in Hs if H.rank == 2]
+        prjs = [H for H in Hs if H.rank == 1]
+        mc = np.asarray([c for H, c in zip(Hs, coeffs) if H.rank == 2] or [0.0])
+        pc = np.asarray([c for H, c in zip(Hs, coeffs) if H.rank == 1] or [0.0])
+        mh = (L.P * max(len(mpos), 1))(*[H._h for H in mpos])
+        ph = (L.P * max(len(prjs), 1))(*[H._h for H in prjs])
+        ctx.check(ctx.lib.tn_dmrg_sum(ctx.h, psi._h, len(mpos), mh, L.as_dp(mc), len(prjs), ph,
+                                      L.as_dp(pc), C.byref(o), C.byref(e), C.byref(st)))
     if stats is not None:
         stats.update(sweeps=st.sweeps, maxbonddim=st.maxbonddim, matvecs=st.matvecs,
                      seconds=st.seconds, energy_fp64=st.energy_fp64,

@@ -283,3 +283,38 @@ def test_known_answer_fixtures_are_current():
     for k in fresh:
         assert np.allclose(fresh[k], stored[k], rtol=1e-13, atol=1e-13), k
     assert abs(stored["tfim_open_N20_J1_h0.5_energy"] - X.tfim_free_fermion_energy(20, 1.0, 0.5)) < 1e-12
+
+
+def test_dmrg_sum_of_mpos_and_projector_matches_ed():
+    """dmrg(psi, Hs...; coeffs) (dmrg.jl:128-154): a sum of two MPOs gives the
+    ground energy of their weighted sum, and an MPS term coeff |phi0><phi0|
+    (ProjMPS(phi0, psi; squared=true)) lifts the ground state so that DMRG
+    finds the first excited state."""
+    st = O.spinhalf()
+    N = 8
+    Hxy, Hzz = O.OpList(N), O.OpList(N)
+    for i in range(1, N):
+        Hxy.add(["x", "x"], [i, i + 1], 1.0)
+        Hxy.add(["y", "y"], [i, i + 1], 1.0)
+        Hzz.add(["z", "z"], [i, i + 1], 1.0)
+    W1, W2 = O.mpo_from_oplist(st, Hxy), O.mpo_from_oplist(st, Hzz)
+    kw = dict(maxdim=32, cutoff=1e-12, maxsweeps=8, minsweeps=8, numconverges=np.inf)
+    psi = O.random_mps(2, N, 4, np.random.default_rng(3))
+    psi, E = O.dmrg(psi, [W1, W2], coeffs=[1.0, 0.7], **kw)
+    dense = X.oplist_to_dense(st, Hxy) + 0.7 * X.oplist_to_dense(st, Hzz)
+    assert abs(np.real(E) - np.linalg.eigvalsh(dense)[0]) < 1e-8
+    # excited state of a gapped transverse-field Ising chain
+    H = O.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], -1.0)
+    for i in range(1, N + 1):
+        H.add("x", i, -1.5)
+    W = O.mpo_from_oplist(st, H)
+    ev = np.linalg.eigvalsh(X.oplist_to_dense(st, H))
+    g = O.random_mps(2, N, 4, np.random.default_rng(4))
+    g, E0 = O.dmrg(g, W, **kw)
+    assert abs(np.real(E0) - ev[0]) < 1e-9
+    ex = O.random_mps(2, N, 4, np.random.default_rng(5))
+    ex, E1 = O.dmrg(ex, [W, g], coeffs=[1.0, 20.0], **kw)
+    assert abs(np.real(E1) - ev[1]) < 1e-8
+    assert abs(np.vdot(X.mps_to_dense(g), X.mps_to_dense(ex))) < 1e-5
