@@ -230,17 +230,28 @@ int32_t tn_qjmc_run(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nju
 
 /* ntraj independent trajectories of the run above from the same initial MPS,
  * advanced concurrently by nworkers host threads, each with its own CUDA
- * stream; trajectory t consumes draws[t*ndraws_per_traj ...].  obs_avg gets
- * the trajectory-averaged observables (rows = t=0 and every save_every
- * steps, nobs columns, re/im); njumps_per_traj (optional) the jump counts.
- * The reference runs one trajectory per qjmc_simulation call (qjmc.jl:28);
- * ensembles are this loop. */
+ * stream.  Uniform draws: with draws != NULL trajectory t consumes
+ * draws[t*ndraws_per_traj ...] (the parity mode: explicit streams); with
+ * draws == NULL trajectory t draws from its own counter-based stream under
+ * `seed` (tn_philox_uniforms(seed, t, ...)), ndraws_per_traj values long
+ * (3*nsteps + 3 always suffices).  obs_avg gets the trajectory-averaged
+ * observables (rows = t=0 and every save_every steps, nobs columns, re/im);
+ * njumps_per_traj (optional) the jump counts.  The reference runs one
+ * trajectory per qjmc_simulation call (qjmc.jl:28) with Julia's rand()
+ * (qjmc.jl:64,97,99); ensembles are this loop. */
 int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, int32_t njump,
                       const int32_t* jump_sites, const double* jump_ops, const double* jump_coeffs,
                       int32_t nsteps, double dt, int32_t ntraj, const double* draws,
-                      int64_t ndraws_per_traj, const tn_trunc_opts* trunc, int32_t save_every,
-                      int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
-                      double* obs_avg, int32_t* njumps_per_traj, int32_t nworkers);
+                      int64_t ndraws_per_traj, uint64_t seed, const tn_trunc_opts* trunc,
+                      int32_t save_every, int32_t nobs, const int32_t* obs_sites,
+                      const double* obs_ops, double* obs_avg, int32_t* njumps_per_traj,
+                      int32_t nworkers);
+/* The per-trajectory uniform stream of tn_qjmc_batch: out[k] in [0, 1) is the
+ * top 53 bits of 64-bit word k % 2 of Philox4x32-10 (Salmon et al., SC 2011)
+ * at counter (k / 2 low 32 bits, trajectory, k / 2 high 32 bits, 0) under the
+ * key (seed low 32 bits, seed high 32 bits).  Host only; no reference
+ * counterpart (the reference draws from Julia's global RNG). */
+int32_t tn_philox_uniforms(uint64_t seed, uint32_t trajectory, int64_t n, double* out);
 
 /* ---- unit-level kernels on host buffers (for parity tests) --------------- */
 /* out[a,s1',s2',c'] = sum L[a,w,b] W1[w,s1',s1,w'] W2[w',s2',s2,w''] th[b,s1,s2,c] R[c',w'',c]

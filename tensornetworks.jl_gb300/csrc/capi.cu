@@ -32,9 +32,10 @@ void heff2_noalloc(Ctx* ctx, int64_t cl, int64_t cr, int d, int64_t wl, int64_t 
                    cplx* out);
 void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsites,
                 const double* jops, const double* jcoeffs, int nsteps, double dt, int ntraj,
-                const double* draws, int64_t ndraws_per_traj, const Trunc& t, int save_every,
-                int nobs, const int* obs_sites, const double* obs_ops, double* obs_avg,
-                int* njumps_per_traj, int nworkers);
+                const double* draws, int64_t ndraws_per_traj, uint64_t seed, const Trunc& t,
+                int save_every, int nobs, const int* obs_sites, const double* obs_ops,
+                double* obs_avg, int* njumps_per_traj, int nworkers);
+void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out);
 }  // namespace tn
 
 using namespace tn;
@@ -617,17 +618,24 @@ int32_t tn_qjmc_run(tn_ctx* h, tn_mps* psi, const tn_gates* g, int32_t njump,
 int32_t tn_qjmc_batch(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32_t njump,
                       const int32_t* jump_sites, const double* jump_ops, const double* jump_coeffs,
                       int32_t nsteps, double dt, int32_t ntraj, const double* draws,
-                      int64_t ndraws_per_traj, const tn_trunc_opts* t, int32_t save_every,
-                      int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
-                      double* obs_avg, int32_t* njumps_per_traj, int32_t nworkers) {
+                      int64_t ndraws_per_traj, uint64_t seed, const tn_trunc_opts* t,
+                      int32_t save_every, int32_t nobs, const int32_t* obs_sites,
+                      const double* obs_ops, double* obs_avg, int32_t* njumps_per_traj,
+                      int32_t nworkers) {
     TN_API_BEGIN(h ? &h->c : nullptr)
-    TN_REQUIRE(psi0 && g && draws && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
+    TN_REQUIRE(psi0 && g && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
     TN_REQUIRE(nsteps >= 0 && njump >= 1 && nobs >= 0, "bad counts");
     TN_REQUIRE(nobs == 0 || (obs_sites && obs_ops), "null observables");
     qjmc_batch(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
-               ndraws_per_traj, to_trunc(t), save_every, nobs, obs_sites, obs_ops, obs_avg,
+               ndraws_per_traj, seed, to_trunc(t), save_every, nobs, obs_sites, obs_ops, obs_avg,
                njumps_per_traj, nworkers);
     TN_API_END
+}
+
+int32_t tn_philox_uniforms(uint64_t seed, uint32_t trajectory, int64_t n, double* out) {
+    if (!out || n < 0) return TN_ERR_INVALID;
+    philox_uniforms(seed, trajectory, n, out);
+    return TN_OK;
 }
 
 // ---- unit-level entry points on host buffers ---------------------------------------

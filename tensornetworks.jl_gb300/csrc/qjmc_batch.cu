@@ -1,6 +1,6 @@
 // Concurrent quantum-jump trajectories.  Trajectories are independent
 // (qjmc.jl:28-166 runs one per call); here a pool of host worker threads,
-// each owning a CUDA stream and solver handle, pulls trajectory indices from
+// each owning a CUDA stream, pulls trajectory indices from
 // an atomic counter and runs the single-trajectory driver on its own copy of
 // the initial MPS.  Gates and operators are shared read-only device data.
 // Per-trajectory kernels are small (chi <= 64 at the QJMC sizes), so
@@ -26,11 +26,43 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
                     int nobs, const int* obs_sites, const double* obs_ops, double* obs_out,
                     int max_jumps);
 
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): ten rounds of two 32x32->64 multiplications
+// with the published multipliers and Weyl key increments.
+static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// The uniform stream of trajectory `traj` under `seed`: draw k in [0, 1)
+// from the 64-bit word (k % 2) of Philox4x32-10(counter = (k / 2 low, traj,
+// k / 2 high, 0), key = (seed low, seed high)), its top 53 bits.
+void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out) {
+    for (int64_t k = 0; k < n; k += 2) {
+        uint32_t c[4] = {(uint32_t)(k / 2), traj, (uint32_t)((uint64_t)(k / 2) >> 32), 0u};
+        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        const uint64_t w0 = ((uint64_t)c[1] << 32) | c[0], w1 = ((uint64_t)c[3] << 32) | c[2];
+        out[k] = (double)(w0 >> 11) * (1.0 / 9007199254740992.0);
+        if (k + 1 < n) out[k + 1] = (double)(w1 >> 11) * (1.0 / 9007199254740992.0);
+    }
+}
+
 void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsites,
                 const double* jops, const double* jcoeffs, int nsteps, double dt, int ntraj,
-                const double* draws, int64_t ndraws_per_traj, const Trunc& t, int save_every,
-                int nobs, const int* obs_sites, const double* obs_ops, double* obs_avg,
-                int* njumps_per_traj, int nworkers) {
+                const double* draws, int64_t ndraws_per_traj, uint64_t seed, const Trunc& t,
+                int save_every, int nobs, const int* obs_sites, const double* obs_ops,
+                double* obs_avg, int* njumps_per_traj, int nworkers) {
+    TN_REQUIRE(ndraws_per_traj >= 1, "need at least one draw per trajectory");
     TN_REQUIRE(ntraj >= 1 && nworkers >= 1, "need at least one trajectory and one worker");
     TN_REQUIRE(save_every >= 1, "save_every must be >= 1");
     const int nrows = nsteps / save_every + 1;
@@ -47,6 +79,7 @@ void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsi
     auto worker = [&]() {
         Ctx ctx;
         std::vector<double> local(nout, 0.0), buf(nout, 0.0);
+        std::vector<double> own(draws ? 0 : (size_t)ndraws_per_traj);
         try {
             ctx_init(ctx, device);
             for (;;) {
@@ -68,8 +101,10 @@ void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsi
                     zcopy(&ctx, psi.A[i - 1].c(), psi0->site(i), psi0->size(i));
                 }
                 std::fill(buf.begin(), buf.end(), 0.0);
+                const double* dr = draws ? draws + (size_t)tr * ndraws_per_traj : own.data();
+                if (!draws) philox_uniforms(seed, (uint32_t)tr, ndraws_per_traj, own.data());
                 QjmcResult r = qjmc_run(&psi, g, njump, jsites, jops, jcoeffs, nsteps, dt,
-                                        draws + (size_t)tr * ndraws_per_traj, ndraws_per_traj, t,
+                                        dr, ndraws_per_traj, t,
                                         save_every, nobs, obs_sites, obs_ops, buf.data(),
                                         nsteps + 1);
                 for (size_t k = 0; k < nout; ++k) local[k] += buf[k];

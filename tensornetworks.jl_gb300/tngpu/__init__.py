@@ -11,7 +11,8 @@ model inputs (operator tables, MPO tensors, 4x4 gate exponentials).
 from ._lib import Context, TNError, context, load  # noqa: F401
 from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEBDEnergy,  # noqa: F401
                          TEBDGradProblem, TEBDNorm, TEBDOperators, applygates, dmrg, qjmc_gates,
-                         qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation, shard_range, tebd,
+                         philox_uniforms, qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation,
+                         shard_range, tebd,
                          tebd_grad, trotterize)
 from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
 from .mps import (GMPS, MPO, MPOHandle, entropy, inner, mps_from_record, mps_record,  # noqa: F401

@@ -317,12 +317,15 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 
 
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
-                  draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64):
+                  draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
+                  seed=None, first_traj=0):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,
     averaged single-site observables [rows x terms], jump counts).  ``draws``
     is an (ntraj x m) array of uniforms consumed per trajectory in the
-    reference's order; otherwise they come from ``rand``."""
+    reference's order; with ``seed`` trajectory t draws from its own
+    counter-based stream philox_uniforms(seed, first_traj + t); otherwise
+    the draws come from ``rand``."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -330,12 +333,20 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     gates = GateList(H.length, rows, st.dim, psi.ctx)
     if any(len(s) != 1 for s in jumpops.sites) or any(len(s) != 1 for s in obs.sites):
         raise NotImplementedError("single-site jump operators and observables only")
-    if draws is None:
+    if draws is None and seed is None:
         g = rand if rand is not None else np.random.default_rng()
         draws = g.random((ntraj, 3 * steps + 3))
-    draws = np.ascontiguousarray(draws, dtype=np.float64)
-    if draws.shape[0] != ntraj:
-        raise ValueError("draws must have one row per trajectory")
+    if draws is None and first_traj != 0:
+        # the library numbers its streams from 0: draw shifted ones here
+        draws = np.stack([philox_uniforms(seed, first_traj + t, 3 * steps + 3)
+                          for t in range(ntraj)])
+    if draws is not None:
+        draws = np.ascontiguousarray(draws, dtype=np.float64)
+        if draws.shape[0] != ntraj:
+            raise ValueError("draws must have one row per trajectory")
+        ndraws, dptr, sd = draws.shape[1], L.as_dp(draws), 0
+    else:
+        ndraws, dptr, sd = 3 * steps + 3, None, int(seed)
     jsites = np.asarray([s[0] for s in jumpops.sites], dtype=np.int32)
     jops = np.concatenate([L.cplx_f(st.op(o[0])).ravel(order="F") for o in jumpops.ops]).astype(np.complex128)
     jco = np.asarray(jumpops.coeffs, dtype=np.complex128)
@@ -349,7 +360,7 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     ctx = psi.ctx
     ctx.check(ctx.lib.tn_qjmc_batch(
         ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
-        L.as_dp(jco), steps, float(dt), ntraj, L.as_dp(draws), draws.shape[1], C.byref(t), savesteps,
+        L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, C.byref(t), savesteps,
         len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
         nj.ctypes.data_as(L.i32p), int(workers)))
     tt, times = 0.0, [0.0]
@@ -360,6 +371,17 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     return times, out, nj
 
 
+def philox_uniforms(seed, trajectory, n):
+    """The uniform stream of one trajectory under ``seed`` (tn_philox_uniforms:
+    Philox4x32-10, Salmon et al. 2011), n values in [0, 1)."""
+    out = np.zeros(int(n))
+    lib = L.load()
+    rc = lib.tn_philox_uniforms(int(seed), int(trajectory), int(n), L.as_dp(out))
+    if rc != L.TN_OK:
+        raise L.TNError(rc, "tn_philox_uniforms failed")
+    return out
+
+
 def shard_range(ntraj, rank, world):
     """Contiguous block of trajectory indices [lo, hi) for one rank: the
     first ntraj % world ranks take one extra trajectory."""
@@ -368,40 +390,68 @@ def shard_range(ntraj, rank, world):
     return lo, lo + base + (1 if rank < extra else 0)
 
 
-def qjmc_ensemble_sharded(st, psi, H, jumpops, tmax, dt, obs, ntraj, draws, group=None,
-                          run=None, **kw):
+_HOST_GROUPS = {}
+
+
+def _host_group(group):
+    """A gloo process group over the ranks of ``group`` for the host-tensor
+    reduction (an NCCL group carries device tensors only); created once,
+    collectively, the first time a non-gloo group asks."""
+    import torch.distributed as dist
+    if dist.get_backend(group) == "gloo":
+        return group
+    key = "world" if group is None else id(group)
+    if key not in _HOST_GROUPS:
+        ranks = None if group is None else dist.get_process_group_ranks(group)
+        _HOST_GROUPS[key] = dist.new_group(ranks=ranks, backend="gloo")
+    return _HOST_GROUPS[key]
+
+
+def qjmc_ensemble_sharded(st, psi, H, jumpops, tmax, dt, obs, ntraj, draws=None, group=None,
+                          run=None, seed=None, **kw):
     """qjmc_ensemble with the trajectories sharded over the ranks of a
     torch.distributed process group (one process per GPU).  Each rank runs
-    its block of trajectories (draw rows lo:hi) with no data-path
-    collective; the trajectory-summed observables and the per-trajectory
-    jump counts are combined once at the end (all_reduce / all_gather on the
-    host).  Returns what qjmc_ensemble returns for all ntraj trajectories.
-    ``run`` replaces qjmc_ensemble (same signature), for host-only tests."""
+    its block of trajectories [lo, hi) -- draw rows lo:hi, or with ``seed``
+    the streams philox_uniforms(seed, lo..hi-1), the same trajectories one
+    process would run -- with no data-path collective; the
+    trajectory-summed observables and the per-trajectory jump counts are
+    combined once at the end (all_reduce / all_gather on the host, over a
+    gloo group when ``group`` is an NCCL group).  Returns what qjmc_ensemble
+    returns for all ntraj trajectories.  ``run`` replaces qjmc_ensemble (same
+    signature), for host-only tests."""
     import torch
     import torch.distributed as dist
     run = run or qjmc_ensemble
     world = dist.get_world_size(group) if dist.is_initialized() else 1
     rank = dist.get_rank(group) if dist.is_initialized() else 0
     lo, hi = shard_range(ntraj, rank, world)
-    draws = np.asarray(draws)
+    if draws is None and seed is None:
+        raise ValueError("give draws or a seed")
+
+    def block(a, b):
+        if draws is not None:
+            return dict(draws=np.asarray(draws)[a:b])
+        return dict(seed=seed, first_traj=a)
+
     if hi > lo:
-        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, hi - lo, draws=draws[lo:hi], **kw)
+        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, hi - lo, **block(lo, hi), **kw)
         part = np.asarray(avg, dtype=np.complex128) * (hi - lo)
     else:
-        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, 1, draws=draws[:1], **kw)
+        times, avg, nj = run(st, psi, H, jumpops, tmax, dt, obs, 1, **block(0, 1), **kw)
         part = np.zeros_like(np.asarray(avg, dtype=np.complex128))
         nj = np.zeros(0, dtype=np.int32)
     if world == 1:
         return times, part / ntraj, np.asarray(nj, dtype=np.int32)
+    hg = _host_group(group)
     buf = torch.from_numpy(np.ascontiguousarray(part.view(np.float64)))
-    dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=hg)
     total = buf.numpy().view(np.complex128).reshape(part.shape)
     # equal-size gather (padded to the largest block), trimmed per rank
     m = -(-int(ntraj) // world)
     mine = np.full(m, -1, dtype=np.int32)
     mine[:hi - lo] = np.asarray(nj, dtype=np.int32)[:hi - lo]
     counts = [torch.zeros(m, dtype=torch.int32) for _ in range(world)]
-    dist.all_gather(counts, torch.from_numpy(mine), group=group)
+    dist.all_gather(counts, torch.from_numpy(mine), group=hg)
     sizes = [shard_range(ntraj, r, world)[1] - shard_range(ntraj, r, world)[0] for r in range(world)]
     return times, total / ntraj, np.concatenate([c.numpy()[:k] for c, k in zip(counts, sizes)])
 

@@ -164,3 +164,17 @@ def test_mps_checkpoint_record_round_trip(tmp_path):
     bad["state/type"] = np.array("MPO")
     with pytest.raises(ValueError, match="does not contain MPS data"):
         M.mps_from_record(bad, name="state")
+
+
+def test_philox_stream_matches_oracle():
+    """tn_philox_uniforms (the seeded QJMC streams) against the oracle's
+    restatement of Philox4x32-10, across seeds, trajectories and lengths."""
+    from oracle.philox import trajectory_uniforms
+    import tngpu as tn
+    for seed in (0, 4, 2 ** 40 + 17):
+        for traj in (0, 1, 1023):
+            for n in (1, 7, 64):
+                a = tn.philox_uniforms(seed, traj, n)
+                b = trajectory_uniforms(seed, traj, n)
+                assert np.array_equal(a, b)
+                assert np.all((a >= 0.0) & (a < 1.0))

@@ -318,3 +318,15 @@ def test_dmrg_sum_of_mpos_and_projector_matches_ed():
     ex, E1 = O.dmrg(ex, [W, g], coeffs=[1.0, 20.0], **kw)
     assert abs(np.real(E1) - ev[1]) < 1e-8
     assert abs(np.vdot(X.mps_to_dense(g), X.mps_to_dense(ex))) < 1e-5
+
+
+def test_philox4x32_10_known_answers():
+    """The oracle's Philox4x32-10 against the generator's published
+    known-answer vectors (Salmon et al., SC 2011)."""
+    from oracle.philox import philox4x32_10
+    kats = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+            ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+            ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+             (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for c, k, e in kats:
+        assert philox4x32_10(c, k) == e
