@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=N_SITES)
     p.add_argument("--chi", type=int, default=CHI)
+    p.add_argument("--mode", default="mixed", choices=["mixed", "mixed-env64"],
+                   help="precision mode of the timed sweeps: 3xTF32 H_eff, environments and "
+                        "projections (mixed), or the same with FP64 environment updates")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-side", action="store_true", help="skip the QJMC and TEBD samples")
@@ -189,6 +192,21 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
+def sweep_flops(dims, d=2, w=5, n_mv=5):
+    """Algorithmic flops of one directional sweep over the bonds of an MPS
+    with bond dimensions `dims` (N+1 entries): per bond n_mv two-site H_eff
+    products, one environment update and the truncation products (the
+    eigensolver excluded), 8 flops per complex multiply-add."""
+    tot = 0.0
+    for i in range(len(dims) - 2):
+        cl, cr, k = dims[i], dims[i + 2], dims[i + 1]
+        f_mv = 8.0 * (w * d * d * cl * cl * cr + 2 * w * w * d ** 3 * cl * cr + w * d * d * cl * cr * cr)
+        f_env = 8.0 * (w * d * cl * cl * cr + w * w * d * d * cl * cr + w * d * cl * cr * cr)
+        f_tr = 8.0 * ((d * cl) ** 2 * (d * cr) + (d * cl) * (d * cr) * k)
+        tot += n_mv * f_mv + f_env + f_tr
+    return tot
+
+
 def ours(args):
     import ctypes as C
 
@@ -211,7 +229,7 @@ def ours(args):
     for md in (64, 256):
         t0 = time.perf_counter()
         tn.dmrg(psi, W_mpo, maxdim=md, cutoff=1e-12, minsweeps=2, maxsweeps=2, numconverges=np.inf,
-                verbose=False, precision="mixed")
+                verbose=False, precision=args.mode)
         ramp[md] = time.perf_counter() - t0
 
     Wu, K = args.warmup, args.steps
@@ -220,16 +238,15 @@ def ours(args):
     clk = Clocks(local)
     st = {}
     t0 = time.perf_counter()
-    # an even number of directional sweeps leaves the centre at site 1, so the
-    # FP64 sample and the end-to-end run start without re-canonicalising; a
-    # padding sweep joins the warm-ups so the timed sweeps are the last K
-    pad = (Wu + K) % 2
+    # the timed sweeps run with the profiler off; one profiled sweep follows
+    # them.  An even total leaves the centre at site 1 for the end-to-end run
+    # (a padding sweep joins the warm-ups).
+    pad = (Wu + K + 1) % 2
     Wu_eff = Wu + pad
-    total = Wu_eff + K
-    _, E = tn.dmrg(psi, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=total,
-                   maxsweeps=total,
-                   numconverges=np.inf, verbose=False, precision="mixed", stats=st,
-                   profile_from_sweep=Wu_eff)
+    total = Wu_eff + K + 1
+    kw = dict(maxdim=args.chi, mindim=args.chi, cutoff=1e-12, numconverges=np.inf, verbose=False)
+    _, E = tn.dmrg(psi, W_mpo, minsweeps=total, maxsweeps=total, precision=args.mode, stats=st,
+                   profile_from_sweep=Wu_eff + K, **kw)
     wall_main = time.perf_counter() - t0
     clocks = clk.stop()
     log(f"main: {wall_main:.1f} s, sweeps {['%.2f' % s for s in st['sweep_seconds']]}, "
@@ -243,69 +260,73 @@ def ours(args):
         t_timed = float(tt.item())
     value = world * K / t_timed
 
-    # kernel profile of the timed sweeps
-    n = L.TN_PROF if hasattr(L, "TN_PROF") else 8
+    # kernel profile of the profiled sweep (CUDA events on the library's
+    # stream around every launch)
+    n = 8
     la, ms, fl, by = (C.c_int64 * n)(), (C.c_double * n)(), (C.c_double * n)(), (C.c_double * n)()
     ctx.check(ctx.lib.tn_profile_read(ctx.h, la, ms, fl, by))
     prof = [{"kernel": L.PROF_CLASSES[i], "launches": int(la[i]), "ms": ms[i], "flops": fl[i],
              "bytes": by[i]} for i in range(n)]
-    gpu_launches = int(la[7])
+    gpu_launches = int(la[7]) * K  # launches of the profiled sweep, per timed sweep
     ph = (C.c_double * 4)()
     ctx.check(ctx.lib.tn_profile_phases(ctx.h, ph))
     phases = dict(zip(("environment", "two_site_prep", "lanczos", "truncation"), list(ph)))
+    log("profile (one sweep): " + json.dumps(prof))
 
     pk, pk_src = peaks()
-    tf32_peak = 0.5 * pk["bf16_tflops"]
+    tf32_peak = 0.5 * pk.get("bf16_tflops_sustained", pk["bf16_tflops"])
+    z_peak = cublas_zgemm_tflops(local)
     tc = prof[0]
     tc_achieved = 3.0 * tc["flops"] / (tc["ms"] * 1e-3) / 1e12 if tc["ms"] > 0 else 0.0
     roof_tc = {"kernel": tc["kernel"], "bound": "tensor", "achieved": tc_achieved, "peak": tf32_peak,
                "unit": "TFLOP/s", "frac": tc_achieved / tf32_peak,
-               # dram bytes read + written by one bulk-shape launch (L . theta,
-               # 5120 x 4096 x 1024) in an ncu capture: 151 MB + 1282 MB
-               "traffic": 1.433e9, "traffic_note": "one ncu capture of the bulk-shape H_eff GEMM; "
-                                                   "writes are the split-K FP32 partials",
                "launches": tc["launches"], "avg_launch_ms": tc["ms"] / max(tc["launches"], 1),
                "note": "achieved counts the three TF32 passes the tensor pipe executes "
                        "(3 x 8 flops per complex multiply-add); peak = 0.5 x "
-                       f"{pk_src} bf16 dense ({pk['bf16_tflops']} TF/s): TF32 runs at half the "
-                       "BF16 rate"}
-    own = [p for i, p in enumerate(prof) if i not in (2, 7)]
+                       f"{pk_src} sustained bf16 dense: TF32 runs at half the BF16 rate"}
+    own = [p for i, p in enumerate(prof) if i != 7]
     dom = max(own, key=lambda p: p["ms"])
-    roof = roof_tc
-    if dom is not tc and dom["kernel"].startswith("zgemm"):
-        # FP64 SIMT GEMM: the FP64 peak is not in the measured-peaks file;
-        # cuBLAS ZGEMM 4096^3 is timed here as the denominator
-        z_peak = cublas_zgemm_tflops(local)
+    kern_ms = sum(p["ms"] for p in own)
+    if dom is tc:
+        roof = dict(roof_tc)
+    else:
         ach = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
         roof = {"kernel": dom["kernel"], "bound": "fp64-pipe", "achieved": ach, "peak": z_peak,
                 "unit": "TFLOP/s", "frac": ach / z_peak if z_peak else None,
-                # dram bytes read + written by the bulk Gram launch (2048^3,
-                # lower triangle) in an ncu capture: 96 MB + 14 MB
-                "traffic": 1.106e8, "traffic_note": "one ncu capture of the bulk-shape Gram launch; "
-                                                    "the FP64 pipe is 99.6 % active",
                 "launches": dom["launches"], "avg_launch_ms": dom["ms"] / max(dom["launches"], 1),
-                "note": "peak = cuBLAS ZGEMM 4096^3 measured in this run (the measured-peaks file "
-                        "has no FP64 figure)"}
+                "note": "FP64 SIMT kernels: peak = cuBLAS ZGEMM 4096^3 timed in this run (the "
+                        "measured-peaks file has no FP64 figure); achieved = the class's "
+                        "algorithmic flops (eigensolver: 16/3 n^3 + 8 n^2 k per call, the "
+                        "LAPACK count) over its event time"}
+    roof["share_of_kernel_time"] = dom["ms"] / kern_ms if kern_ms else None
+    roof["traffic"] = None
+    f_sweep = sweep_flops(psi.bonddims())
+    sweep_roof = {"algorithmic_tflops_per_s": f_sweep / (t_timed / K) / 1e12, "peak_tf32": tf32_peak,
+                  "frac": f_sweep / (t_timed / K) / 1e12 / tf32_peak, "sweep_flops": f_sweep,
+                  "note": "per bond 5 H_eff products + environment update + truncation products "
+                          "(eigensolver excluded) at the actual bond dims, over ms_per_step"}
 
-    # FP64 comparison: bond-update sample of the same state, plain FP64 path
-    log("profile: " + json.dumps(prof))
-    log("phases (s over the timed sweeps): " + json.dumps(phases))
-    fp64 = fp64_sample(tn, psi, W_mpo, args, st)
-    log("fp64 sample: " + json.dumps(fp64))
+    acc = accuracy_arms(tn, psi, W_mpo, kw)
+    log("accuracy: " + json.dumps(acc))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": Wu, "ms_per_step": 1e3 * t_timed / K, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "mixed(tf32x3 tensor-core, f64)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": f"{args.mode} (tf32x3 tensor-core products, f64 Lanczos/eigensolver)",
             "data": "synthetic", "config": config(args), "clocks": clocks,
             "gpu_launches": gpu_launches, "roofline": roof, "roofline_tensor_core": roof_tc,
+            "roofline_sweep": sweep_roof, "mode": args.mode,
             "energy": {"returned": E, "fp64_rayleigh": st["energy_fp64"],
                        "last_sweep_lanczos": st["sweep_energies"][total - 1]},
+            "accuracy": acc, "rel_err_vs_fp64": acc[args.mode]["rel_err_vs_fp64"],
+            "fp64": {"sweeps_per_s": acc["fp64_sweeps_per_s"], "sweep_s": acc["fp64_sweep_s"],
+                     "method": "one plain-FP64 sweep at maxdim=mindim=chi from the same state, "
+                               "device events at the sweep boundaries"},
+            "mixed_vs_fp64": value / world / acc["fp64_sweeps_per_s"],
             "sweeps": {"seconds": st["sweep_seconds"], "maxdim": st["sweep_maxdim"],
                        "energies": st["sweep_energies"], "ramp_seconds": ramp,
-                       "main_wall_s": wall_main},
-            "fp64": fp64, "kernel_profile": prof, "phase_seconds": phases}
-    if fp64.get("sweeps_per_s_est"):
-        line["mixed_vs_fp64"] = value / world / fp64["sweeps_per_s_est"]
+                       "main_wall_s": wall_main, "profiled_sweep": Wu_eff + K},
+            "kernel_profile": prof, "phase_seconds": phases}
     if not args.no_e2e:
         line["e2e"] = e2e_run(tn, ctx, psi, W_mpo, args, world)
         log("e2e: " + json.dumps(line["e2e"]))
@@ -324,6 +345,7 @@ def ours(args):
         t = cpu_bond_sample(args.chi)
         line["cpu_baseline"] = {"value": 1.0 / (t * (args.n - 1)), "unit": UNIT,
                                 "cores": os.cpu_count(), "kind": "port",
+                                "blas_threads": os.environ.get("OPENBLAS_NUM_THREADS", "default"),
                                 "sample": f"one bond update at chi={args.chi} ({t:.1f} s: 5 Lanczos "
                                           f"matvecs, SVD, env update), x{args.n - 1} bonds; numpy "
                                           "FP64 restatement (Julia absent)"}
@@ -332,6 +354,30 @@ def ours(args):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def accuracy_arms(tn, psi, W_mpo, kw, modes=("mixed", "mixed-env64")):
+    """From copies of the same state: one plain-FP64 sweep (its last local
+    Lanczos eigenvalue, as dmrg.jl:55,98 returns, and the FP64 <psi|H|psi> of
+    its final state) and one sweep in each mixed mode (whose returned energy
+    is the FP64 <psi|H|psi> of its final state).  |dE/E| compares the final
+    states' FP64 energies; each mixed arm's in-sweep Lanczos value is
+    reported beside them."""
+    pf, sf = psi.copy(), {}
+    _, Ef = tn.dmrg(pf, W_mpo, minsweeps=1, maxsweeps=1, precision="fp64", stats=sf, **kw)
+    E64, t64 = sf["energy_fp64"], sf["sweep_seconds"][0]
+    out = {"fp64_energy": E64, "fp64_last_lanczos": Ef, "fp64_sweep_s": t64,
+           "fp64_sweeps_per_s": 1.0 / t64, "fp64_maxdim": pf.maxbonddim()}
+    for mode in modes:
+        pm, sm = psi.copy(), {}
+        _, Em = tn.dmrg(pm, W_mpo, minsweeps=1, maxsweeps=1, precision=mode, stats=sm, **kw)
+        out[mode] = {"energy_fp64": Em, "rel_err_vs_fp64": abs(Em - E64) / abs(E64),
+                     "last_lanczos": sm["sweep_energies"][0],
+                     "lanczos_rel_dev_from_its_fp64": abs(sm["sweep_energies"][0] - Em) / abs(Em),
+                     "sweep_s": sm["sweep_seconds"][0], "maxdim": pm.maxbonddim(),
+                     "bonddims_identical_to_fp64": pm.bonddims() == pf.bonddims()}
+        del pm
+    return out
 
 
 def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=256, workers=64):
@@ -425,35 +471,16 @@ def cublas_zgemm_tflops(device):
         return None
 
 
-def fp64_sample(tn, psi, W_mpo, args, st_mixed, nbonds=14):
-    """Plain FP64 DMRG bond updates from the chi=1024 state: the first
-    `nbonds` of a right sweep (the last of them at the bulk chi).  The FP64
-    sweep time is the measured time of those bonds plus, for every other
-    bond, the bulk per-bond time scaled by (chi_bond / chi_bulk)^3."""
-    p = psi.copy()
-    st = {}
-    tn.dmrg(p, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=1, maxsweeps=1,
-            numconverges=np.inf, verbose=False, precision="fp64", stats=st, max_bond_updates=nbonds)
-    secs, chis = np.asarray(st["bond_seconds"]), np.asarray(st["bond_chi"])
-    bulk = secs[chis == chis.max()]
-    per_bulk = float(bulk[1:].mean() if bulk.size > 1 else bulk.mean())
-    dims = psi.bonddims()
-    chi_b = [max(dims[i], dims[i + 2]) for i in range(len(dims) - 2)]
-    est = float(secs.sum()) + sum(per_bulk * (c / chis.max()) ** 3 for c in chi_b[len(secs):])
-    return {"bond_seconds": secs.tolist(), "bond_chi": chis.tolist(), "bulk_bond_s": per_bulk,
-            "bulk_chi": int(chis.max()), "sweep_s_est": est, "sweeps_per_s_est": 1.0 / est,
-            "method": f"{nbonds} FP64 bond updates measured; remaining bonds = bulk time x "
-                      "(chi/chi_bulk)^3"}
-
-
 def e2e_run(tn, ctx, psi, W_mpo, args, world):
-    """K sweeps through the C ABI from pinned host buffers: upload the MPS,
-    tn_dmrg (mixed, K sweeps), download the MPS, all inside the timed region."""
+    """Sweeps through the C ABI from pinned host buffers: upload the MPS,
+    tn_dmrg (min(K, 2) sweeps in the bench's mode), download the MPS, all
+    inside the timed region (the sweep count is bounded to keep the run
+    within minutes)."""
     import ctypes as C
 
     import torch
     from tngpu import _lib as L
-    K = args.steps
+    K = min(args.steps, 2)
     ts = psi.tensors()
     pinned = [torch.empty(t.size * 2, dtype=torch.float64, pin_memory=True) for t in ts]
     views = []
@@ -472,7 +499,7 @@ def e2e_run(tn, ctx, psi, W_mpo, args, world):
     st = {}
     tn.dmrg(g, W_mpo, maxdim=args.chi, mindim=args.chi, cutoff=1e-12, minsweeps=K, maxsweeps=K,
             numconverges=np.inf,
-            verbose=False, precision="mixed", stats=st)
+            verbose=False, precision=args.mode, stats=st)
     t_dmrg = time.perf_counter() - t0 - t_up
     out = g.bonddims()
     outs = []
