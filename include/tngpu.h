@@ -175,6 +175,37 @@ int32_t tn_dmrg_sum(tn_ctx* ctx, tn_mps* psi, int32_t nmpo, const tn_mpo* const*
                     const double* proj_coeffs, const tn_dmrg_opts* opts, double* energy,
                     tn_dmrg_stats* stats);
 
+/* ---- variational fitting and MPO products (vmps.jl, mpo.jl, projector.jl) -- */
+/* Keywords of vmps (src/algorithms/mps/vmps.jl:2-13). */
+typedef struct tn_vmps_opts {
+    int32_t nsites;        /* must be 2                                   */
+    int32_t minsweeps;     /* default 2                                   */
+    int32_t maxsweeps;     /* default 200; 0 = unlimited                  */
+    double tol;            /* default 1e-10                               */
+    double numconverges;   /* default 3                                   */
+    double cutoff;         /* default 1e-12                               */
+    int64_t maxdim;        /* default 1000                                */
+    int64_t mindim;        /* default 1                                   */
+    int32_t verbose;
+} tn_vmps_opts;
+/* vmps(psis...) (vmps.jl:1-105): a new MPS, initially a copy of terms[0]
+ * centred at site 1, fitted by two-site sweeps to sum_k coeffs[k] |terms[k]>
+ * (coeffs: nterms complex (re, im) pairs, NULL = all 1; the reference
+ * carries a weight inside the term's scaled tensor).  *cost receives the
+ * final |fit|^2 - 2 |<target|fit>| (vmps.jl:18-25), *sweeps the count. */
+int32_t tn_vmps(tn_ctx* ctx, int32_t nterms, const tn_mps* const* terms, const double* coeffs,
+                const tn_vmps_opts* opts, tn_mps** out, double* cost, int32_t* sweeps);
+/* applyMPO(O, psi; kwargs) = MPOMPSProduct (mpo.jl:125-146): a new MPS with
+ * bond dimensions w_i * D_i, left-canonicalised, then its centre moved to
+ * site 1 with the truncation trunc (NULL: none). */
+int32_t tn_mpo_apply(tn_ctx* ctx, const tn_mpo* O, const tn_mps* psi, const tn_trunc_opts* trunc,
+                     tn_mps** out);
+/* psi <- a psi, a complex (re, im): the centre tensor is scaled (site 1
+ * without a centre), as *(psi, a) does (abstractmps.jl:100-107). */
+int32_t tn_mps_scale(tn_ctx* ctx, tn_mps* psi, const double* a);
+/* <bra|ket> (inner(phi, psi), mpo.jl:181-250 with two MPSs); out = (re, im). */
+int32_t tn_mps_overlap(tn_ctx* ctx, const tn_mps* bra, const tn_mps* ket, double* out);
+
 /* ---- gates (structures/mps/gatelist.jl) ----------------------------------- */
 /* nrows rows; row r has row_len[r] gates; sites/gate_nsites/gate_ptrs list all
  * gates row after row.  gate_ptrs[g] is [o1,i1,o2,i2] (2 sites) or [o,i]. */

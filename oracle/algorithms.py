@@ -8,13 +8,13 @@ import math
 import numpy as np
 import scipy.linalg as sla
 
-from .core import (ProjMPSSum, GMPS, OpList, ProjMPS, applyop, fr, inner, siterange,
+from .core import (MPSProjector, ProjMPSSum, mpo_mps_product, GMPS, OpList, ProjMPS, applyop, fr, inner, siterange,
                    sitetensor)
 
 __all__ = [
     "lanczos_lowest", "dmrg", "trotterize", "applygate", "applygates", "tebd",
     "qjmc_gates", "qjmc_emission_rates", "qjmc_simulation", "dmrg_sweep_stats",
-    "tebd_segments_objective",
+    "tebd_segments_objective", "vmps", "apply_op",
 ]
 
 
@@ -255,9 +255,75 @@ def applygates(psi, rows, cutoff=0.0, maxdim=0, mindim=1):
             applygate(psi, sites[g], gates[g], direction, cutoff, maxdim, mindim)
 
 
+def vmps(*psis, coeffs=None, nsites=2, minsweeps=2, maxsweeps=200, tol=1e-10, numconverges=3,
+         cutoff=1e-12, maxdim=1000, mindim=1, stats=None):
+    """vmps(psis...; kwargs) (vmps.jl:1-105): psi0 = a copy of psis[0] centred
+    at 1, fitted by two-site sweeps to sum_k coeffs[k] psis[k] (the reference
+    weights by scaling a term's tensor: the same target).  At each bond the
+    local target is sum_k c_k conj(project(ProjMPS(psi_k, psi0))) and
+    replacesites! splits it without normalising; the cost is |psi0|^2 -
+    2 |calculate| and converged sweeps accumulate as the reference's do."""
+    psi0 = psis[0].copy()
+    psi0.movecenter(1)
+    N = len(psi0)
+    cs = [1.0] * len(psis) if coeffs is None else list(coeffs)
+    projs = [ProjMPS(p, psi0, None, center=1) for p in psis]
+
+    def cost():
+        nrm = abs(psi0.norm()) ** 2
+        c = sum(np.conj(ck) * p.calculate() for ck, p in zip(cs, projs))
+        return nrm - 2 * abs(c)
+
+    def diff(x, y):
+        return abs(x - y) if abs(x) < 1e-10 else abs((x - y) / x)
+
+    lastcost = cost()
+    lastD = psi0.maxbonddim()
+    direction, converged, convsweeps, sweeps = False, False, 0, 0
+    while not converged:
+        for j in range(1, N + 2 - nsites):
+            site = N + 1 - j if direction else j
+            site1 = site + 1 - nsites if direction else site
+            for p in projs:
+                p.movecenter(site)
+            vec = sum(ck * np.conj(p.project(direction)) for ck, p in zip(cs, projs))
+            psi0.replacesites(vec, site1, direction, False, cutoff=cutoff, maxdim=maxdim,
+                              mindim=mindim)
+        for p in projs:
+            p.movecenter(1 if direction else N)
+        direction = not direction
+        sweeps += 1
+        D = psi0.maxbonddim()
+        c = cost()
+        if sweeps >= minsweeps:
+            if diff(c, lastcost) < tol and lastD == D:
+                convsweeps += 1  # never reset: vmps.jl:67 compares instead of assigning
+            if convsweeps >= numconverges:
+                converged = True
+            if sweeps >= maxsweeps and maxsweeps != 0:
+                converged = True
+        lastcost, lastD = c, D
+    if stats is not None:
+        stats.update(cost=lastcost, sweeps=sweeps)
+    return psi0
+
+
+def apply_op(P, psi, **kw):
+    """P * psi for an MPSProjector or an MPO (applyMPO, projector.jl:41-47,
+    mpo.jl:105-146)."""
+    if isinstance(P, MPSProjector):
+        return P.apply(psi)
+    return mpo_mps_product(P, psi, **kw)
+
+
 def tebd(st, psi, H, dt, tmax, save, observers=None, cutoff=1e-12, maxdim=0,
-         mindim=1, evol="imag", order=2, norm=0.0, record=None):
-    """TEBD step loop without projectors (tebd.jl:3-100).
+         mindim=1, evol="imag", order=2, norm=0.0, record=None, projectors=None,
+         projection_every=10, variational_cutoff=None):
+    """TEBD step loop (tebd.jl:3-100).  ``projectors`` (MPS, MPO or
+    MPSProjector) are projected out before the loop and after every
+    ``projection_every`` steps by psi = vmps(psi, -P psi, ...) at
+    ``variational_cutoff`` and ``maxdim`` (tebd.jl:23-41,67-73); the
+    returned psi is then a new MPS.
 
     ``observers`` is a list of OpList; their expectations are appended to
     ``record`` (dict with 'times', 'ops', 'lognorm', 'energy') at t=0 and
@@ -268,6 +334,16 @@ def tebd(st, psi, H, dt, tmax, save, observers=None, cutoff=1e-12, maxdim=0,
     if len(psi) != H.length:
         raise ValueError("OpList and MPS have different lengths.")
     rows = trotterize(st, H, dt, order=order, evol=evol)
+    vcut = cutoff if variational_cutoff is None else variational_cutoff
+    projs = [MPSProjector(p, p) if (hasattr(p, "rank") and p.rank == 1) else p
+             for p in (projectors or [])]
+
+    def project(p):
+        terms = [p] + [apply_op(P, p) for P in projs]
+        return vmps(*terms, coeffs=[1.0] + [-1.0] * len(projs), cutoff=vcut, maxdim=maxdim)
+
+    if projs:
+        psi = project(psi)
     nsteps = int(round(tmax / dt))
     save = dt if save < dt else save
     nsave = int(round(save / dt))
@@ -288,6 +364,8 @@ def tebd(st, psi, H, dt, tmax, save, observers=None, cutoff=1e-12, maxdim=0,
     psi.norm()  # tebd.jl:61 evaluates log(norm(psi)), which canonicalises an unset centre
     while True:
         applygates(psi, rows, cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+        if projs and (step + 1) % projection_every == 0:
+            psi = project(psi)
         normal += math.log(float(np.real(psi.norm())))
         psi.normalize()
         step += 1

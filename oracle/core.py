@@ -14,6 +14,7 @@ __all__ = [
     "Sitetypes", "spinhalf", "OpList", "svd_keep", "trunc_svd", "GMPS",
     "random_mps", "product_mps", "mpo_from_oplist", "ProjMPS", "inner",
     "applyop", "totensor", "sitetensor", "siterange", "siteindexs", "fr",
+    "ProjMPSSum", "overlap", "scaled", "mpo_mps_product", "MPSProjector",
 ]
 
 
@@ -619,6 +620,58 @@ class ProjMPS:
         left = env_left(self.block(site - 1), self.bra[site], self._W(site), self.ket[site])
         right = self.block(site + 1)
         return self.coeff * np.sum(left * right)
+
+
+def overlap(phi, psi):
+    """<phi|psi> of two MPSs (inner(phi, psi), mpo.jl:181-250)."""
+    L = _edge(2)
+    for i in range(1, len(psi) + 1):
+        L = env_left(L, phi[i], None, psi[i])
+    return complex(L.reshape(-1)[0])
+
+
+def scaled(psi, a):
+    """*(psi, a) (abstractmps.jl:100-107): a copy with the centre tensor
+    (site 1 without a centre) multiplied by a."""
+    phi = psi.copy()
+    site = phi.center if phi.center != 0 else 1
+    phi[site] = phi[site] * a
+    return phi
+
+
+def mpo_mps_product(O, psi, cutoff=0.0, maxdim=0, mindim=1):
+    """MPOMPSProduct(O, psi; kwargs) (mpo.jl:125-146): site tensors
+    phi[(w, a), o, (w', b)] = sum_s O[w, o, s, w'] A[a, s, b] (w fastest in
+    each pair), left-canonicalised by untruncated SVDs while they are built,
+    then, the centre being unset, movecenter!(phi, 1; kwargs) sweeps from N."""
+    N = len(psi)
+    ts = []
+    for i in range(1, N + 1):
+        M, A = O[i], psi[i]
+        B = np.einsum("wosv,asb->waovb", M, A)  # [w, a, o, w', b]
+        wl, al, d, wr, ar = B.shape
+        ts.append(B.reshape(wl * al, d, wr * ar, order="F"))
+    phi = GMPS(1, psi.dim, ts, 0)
+    for i in range(1, N):
+        phi.moveright(i)
+    phi.center = 0
+    phi.movecenter(1, cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+    return phi
+
+
+class MPSProjector:
+    """|right><left| / constant (projector.jl:1-47), constant = <left|right>
+    unless given."""
+
+    rank = 2
+
+    def __init__(self, left, right=None, constant=0.0):
+        self.left = left
+        self.right = left if right is None else right
+        self.constant = complex(constant) if constant != 0.0 else overlap(self.left, self.right)
+
+    def apply(self, psi):
+        return scaled(self.right, overlap(self.left, psi) / self.constant)
 
 
 class ProjMPSSum:

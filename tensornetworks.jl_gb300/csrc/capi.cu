@@ -36,6 +36,15 @@ void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsi
                 int save_every, int nobs, const int* obs_sites, const double* obs_ops,
                 double* obs_avg, int* njumps_per_traj, int nworkers);
 void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out);
+struct VmpsResult {
+    double cost;
+    int sweeps;
+};
+VmpsResult vmps_run(tn_mps* fit, const std::vector<const tn_mps*>& terms,
+                    const std::vector<cplx>& coeffs, const tn_vmps_opts& o);
+void mpo_apply(const tn_mpo* O, const tn_mps* psi, const Trunc& t, tn_mps* out);
+void mps_scale(tn_mps* psi, cplx a);
+cplx mps_overlap(const tn_mps* bra, tn_mps* ket);
 }  // namespace tn
 
 using namespace tn;
@@ -426,6 +435,74 @@ int32_t tn_dmrg(tn_ctx* h, tn_mps* psi, const tn_mpo* H, const tn_dmrg_opts* opt
     terms.H.push_back(H);
     terms.hc.push_back(1.0);
     dmrg_run(psi, terms, *opts, energy, stats);
+    TN_API_END
+}
+
+int32_t tn_vmps(tn_ctx* h, int32_t nterms, const tn_mps* const* terms, const double* coeffs,
+                const tn_vmps_opts* opts, tn_mps** out, double* cost, int32_t* sweeps) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(terms && opts && out && nterms >= 1, "null argument");
+    std::vector<const tn_mps*> ts(terms, terms + nterms);
+    std::vector<cplx> cs(nterms, cmk(1, 0));
+    if (coeffs)
+        for (int k = 0; k < nterms; ++k) cs[k] = cmk(coeffs[2 * k], coeffs[2 * k + 1]);
+    for (const tn_mps* t : ts) TN_REQUIRE(t, "null term");
+    const tn_mps* src = ts[0];
+    tn_mps* fit = new tn_mps();
+    try {
+        fit->ctx = src->ctx;
+        fit->N = src->N;
+        fit->d = src->d;
+        fit->dims = src->dims;
+        fit->center = src->center;
+        fit->A.resize(src->N);
+        for (int i = 1; i <= src->N; ++i) {
+            fit->A[i - 1] = DBuf(src->ctx, sizeof(cplx) * src->size(i));
+            zcopy(src->ctx, fit->A[i - 1].c(), src->site(i), src->size(i));
+        }
+        movecenter(fit, 1, no_trunc());
+        VmpsResult r = vmps_run(fit, ts, cs, *opts);
+        if (cost) *cost = r.cost;
+        if (sweeps) *sweeps = r.sweeps;
+        fit->ctx->sync();
+    } catch (...) {
+        delete fit;
+        throw;
+    }
+    *out = fit;
+    TN_API_END
+}
+
+int32_t tn_mpo_apply(tn_ctx* h, const tn_mpo* O, const tn_mps* psi, const tn_trunc_opts* t,
+                     tn_mps** out) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(O && psi && out, "null argument");
+    tn_mps* r = new tn_mps();
+    try {
+        mpo_apply(O, psi, t ? to_trunc(t) : no_trunc(), r);
+        r->ctx->sync();
+    } catch (...) {
+        delete r;
+        throw;
+    }
+    *out = r;
+    TN_API_END
+}
+
+int32_t tn_mps_scale(tn_ctx* h, tn_mps* psi, const double* a) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(psi && a, "null argument");
+    mps_scale(psi, cmk(a[0], a[1]));
+    psi->ctx->sync();
+    TN_API_END
+}
+
+int32_t tn_mps_overlap(tn_ctx* h, const tn_mps* bra, const tn_mps* ket, double* out) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(bra && ket && out, "null argument");
+    const cplx v = mps_overlap(bra, const_cast<tn_mps*>(ket));
+    out[0] = v.x;
+    out[1] = v.y;
     TN_API_END
 }
 

@@ -13,7 +13,8 @@ from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEB
                          TEBDGradProblem, TEBDNorm, TEBDOperators, applygates, dmrg, qjmc_gates,
                          philox_uniforms, qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation,
                          shard_range, tebd,
-                         tebd_grad, trotterize)
+                         tebd_grad, trotterize, vmps)
 from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
-from .mps import (GMPS, MPO, MPOHandle, entropy, inner, mps_from_record, mps_record,  # noqa: F401
-                  productMPS, randomMPS, read_mps, write_mps)
+from .mps import (GMPS, MPO, MPOHandle, MPSProjector, applyMPO, entropy, inner,  # noqa: F401
+                  mps_from_record, mps_record, overlap, productMPS, randomMPS, read_mps,
+                  write_mps)

@@ -38,6 +38,12 @@ class DmrgOpts(C.Structure):
                 ("verbose", i32), ("max_bond_updates", i32), ("profile_from_sweep", i32)]
 
 
+class VmpsOpts(C.Structure):
+    _fields_ = [("nsites", i32), ("minsweeps", i32), ("maxsweeps", i32), ("tol", f64),
+                ("numconverges", f64), ("cutoff", f64), ("maxdim", i64), ("mindim", i64),
+                ("verbose", i32)]
+
+
 class DmrgStats(C.Structure):
     _fields_ = [("sweeps", i32), ("maxbonddim", i32), ("matvecs", i64), ("seconds", f64),
                 ("energy_fp64", f64), ("last_discarded", f64), ("sweep_cap", i32),
@@ -56,6 +62,11 @@ _SIGS = {
     "tn_mps_bonddims": (i32, [P, P, i64p, i32p]),
     "tn_mps_copy": (i32, [P, P, C.POINTER(P)]),
     "tn_mps_destroy": (i32, [P]),
+    "tn_vmps": (i32, [P, i32, C.POINTER(P), dp, C.POINTER(VmpsOpts), C.POINTER(P), dp,
+                      C.POINTER(i32)]),
+    "tn_mpo_apply": (i32, [P, P, P, C.POINTER(TruncOpts), C.POINTER(P)]),
+    "tn_mps_scale": (i32, [P, P, dp]),
+    "tn_mps_overlap": (i32, [P, P, P, dp]),
     "tn_mpo_upload": (i32, [P, i32, i32, i64p, dpp, C.POINTER(P)]),
     "tn_mpo_destroy": (i32, [P]),
     "tn_mps_movecenter": (i32, [P, P, i32, C.POINTER(TruncOpts)]),

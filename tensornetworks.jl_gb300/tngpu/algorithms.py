@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib as L
 from .models import OpList, trotter_rows, trotter_rows_dparam
-from .mps import GMPS, MPOHandle, inner
+from .mps import GMPS, MPOHandle, MPSProjector, applyMPO, inner
 
 
 # ---------------------------------------------------------------------------
@@ -87,6 +87,30 @@ def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
                      bond_seconds=bsec[: min(st.bond_updates, bcap)].tolist(),
                      bond_chi=bchi[: min(st.bond_updates, bcap)].tolist())
     return psi, e.value
+
+
+def vmps(*psis, coeffs=None, nsites=2, minsweeps=2, maxsweeps=200, tol=1e-10, numconverges=3,
+         cutoff=1e-12, maxdim=1000, mindim=1, verbose=False, stats=None):
+    """vmps(psis...; kwargs) (vmps.jl:1-105): a new MPS, starting as a copy of
+    psis[0] centred at site 1, fitted by two-site sweeps to the sum of the
+    psis (each weighted by ``coeffs``, default 1).  ``stats`` receives the
+    final cost |fit|^2 - 2 |<target|fit>| and the sweep count."""
+    if len(psis) == 0:
+        raise ValueError("vmps needs at least one MPS")
+    ctx = psis[0].ctx
+    cs = [1.0] * len(psis) if coeffs is None else list(coeffs)
+    cbuf = np.zeros(2 * len(psis))
+    for k, c in enumerate(cs):
+        cbuf[2 * k], cbuf[2 * k + 1] = complex(c).real, complex(c).imag
+    o = L.VmpsOpts(nsites, minsweeps, maxsweeps, tol, float(numconverges), cutoff, maxdim,
+                   mindim, int(bool(verbose)))
+    hs = (L.P * len(psis))(*[p._h for p in psis])
+    h, cost, sw = C.c_void_p(), C.c_double(), C.c_int32()
+    ctx.check(ctx.lib.tn_vmps(ctx.h, len(psis), hs, L.as_dp(cbuf), C.byref(o), C.byref(h),
+                              C.byref(cost), C.byref(sw)))
+    if stats is not None:
+        stats.update(cost=cost.value, sweeps=sw.value)
+    return GMPS(h, psis[0].N, psis[0].dim, ctx)
 
 
 # ---------------------------------------------------------------------------
@@ -193,11 +217,17 @@ class TEBDOperators(TEBDObserver):
         self.measurements.append(inner(self.st, psi, self.oplist, psi))
 
 
-def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, maxdim=0,
-         mindim=1, evol="imag", order=2, norm=0.0, verbose=False, precision="fp64"):
-    """Time evolution without projectors (tebd.jl:3-100); returns (psi, energy).
-    precision="mixed" runs the gate contractions and truncation projections
-    as 3xTF32 tensor-core products (FP64 Gram eigensolver and norms)."""
+def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), projectors=(), cutoff=1e-12,
+         maxdim=0, mindim=1, evol="imag", order=2, norm=0.0, verbose=False, precision="fp64",
+         projection_every=10, variational_cutoff=None):
+    """Time evolution (tebd.jl:3-100); returns (psi, energy).  ``projectors``
+    (MPS, MPO handles or MPSProjector) are projected out before the loop and
+    after every ``projection_every`` steps: psi is replaced by vmps(psi,
+    -P_1 psi, ...) at ``variational_cutoff`` (default ``cutoff``) and
+    ``maxdim`` (tebd.jl:23-41,67-73).  ``psi`` may then be a new MPS: use the
+    returned one.  precision="mixed" runs the gate contractions and
+    truncation projections as 3xTF32 tensor-core products (FP64 Gram
+    eigensolver and norms)."""
     if st.dim != psi.dim:
         raise ValueError("Sitetypes and MPS physical dimensions do not match.")
     if len(psi) != H.length:
@@ -207,6 +237,22 @@ def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, m
     if order not in (1, 2):
         raise ValueError("Only first or second order trotter supported.")
     gates = trotterize(st, H, dt, order=order, evol=evol, ctx=psi.ctx)
+    vcut = cutoff if variational_cutoff is None else variational_cutoff
+    projs = []
+    for proj in projectors:
+        if isinstance(proj, GMPS):
+            projs.append(MPSProjector(proj, proj))
+        elif isinstance(proj, (MPOHandle, MPSProjector)):
+            projs.append(proj)
+        else:
+            raise ValueError("Only MPS, MPO and MPSProjectors are supported as projectors.")
+
+    def project(p):
+        terms = [p] + [applyMPO(P, p) for P in projs]
+        return vmps(*terms, coeffs=[1.0] + [-1.0] * len(projs), cutoff=vcut, maxdim=maxdim)
+
+    if projs:
+        psi = project(psi)
     nsteps = int(round(tmax / dt))
     save = dt if save < dt else save
     nsave = int(round(save / dt))
@@ -220,8 +266,18 @@ def tebd(st, psi: GMPS, H: OpList, dt, tmax, save, observers=(), cutoff=1e-12, m
     converged = False
     while not converged:
         ln = C.c_double(0.0)
-        psi.ctx.check(psi.ctx.lib.tn_tebd_steps_prec(psi.ctx.h, psi._h, gates._h, 1, C.byref(t),
-                                                     L.PREC[precision], C.byref(ln)))
+        if projs:
+            # applygates!, the projection every projection_every steps, then
+            # log(norm) and normalize! (tebd.jl:62-78)
+            applygates(psi, gates, cutoff, maxdim, mindim)
+            if (step + 1) % projection_every == 0:
+                psi = project(psi)
+            ln.value = math.log(abs(psi.norm()))
+            psi.normalize()
+        else:
+            psi.ctx.check(psi.ctx.lib.tn_tebd_steps_prec(psi.ctx.h, psi._h, gates._h, 1,
+                                                         C.byref(t), L.PREC[precision],
+                                                         C.byref(ln)))
         normal += ln.value
         step += 1
         converged = step >= nsteps

@@ -116,6 +116,20 @@ class GMPS:
                                                            C.byref(n)))
         return buf[: n.value].copy()
 
+    def scale(self, a):
+        """psi <- a psi in place, the centre tensor scaled (abstractmps.jl:100-107)."""
+        c = (C.c_double * 2)(complex(a).real, complex(a).imag)
+        self.ctx.check(self.ctx.lib.tn_mps_scale(self.ctx.h, self._h, c))
+        return self
+
+    def __mul__(self, a):
+        """*(psi, a): a scaled copy."""
+        if isinstance(a, GMPS):
+            return NotImplemented
+        return self.copy().scale(a)
+
+    __rmul__ = __mul__
+
     def applyop(self, st, ops, sites):
         """applyop! (mps.jl:141-151): A <- O A, no coefficient."""
         if isinstance(ops, str):
@@ -123,6 +137,49 @@ class GMPS:
         for o, s in zip(ops, sites):
             m = L.cplx_f(st.op(o))
             self.ctx.check(self.ctx.lib.tn_mps_applyop(self.ctx.h, self._h, s, L.as_dp(m)))
+
+
+def overlap(phi, psi):
+    """<phi|psi> of two MPSs (inner(phi, psi), mpo.jl:181-250)."""
+    out = (C.c_double * 2)()
+    psi.ctx.check(psi.ctx.lib.tn_mps_overlap(psi.ctx.h, phi._h, psi._h, out))
+    return complex(out[0], out[1])
+
+
+def applyMPO(O, psi, cutoff=0.0, maxdim=0, mindim=1):
+    """applyMPO(O, psi; kwargs) = MPOMPSProduct (mpo.jl:105-146): O|psi> as a
+    new MPS, centred at site 1 after a truncating sweep.  An MPSProjector
+    as O applies (<left|psi>/constant) right (projector.jl:41-47)."""
+    if isinstance(O, MPSProjector):
+        return O.apply(psi)
+    t = L.trunc(cutoff, maxdim, mindim)
+    h = C.c_void_p()
+    psi.ctx.check(psi.ctx.lib.tn_mpo_apply(psi.ctx.h, O._h, psi._h, C.byref(t), C.byref(h)))
+    return GMPS(h, psi.N, psi.dim, psi.ctx)
+
+
+class MPSProjector:
+    """MPSProjector(left, right; constant) (projector.jl:1-47): the operator
+    |right><left| / constant, constant = <left|right> unless given."""
+
+    rank = 2
+
+    def __init__(self, left, right=None, constant=0.0):
+        right = left if right is None else right
+        if left.dim != right.dim:
+            raise ValueError("The MPS must share the same physical dimension.")
+        if len(left) != len(right):
+            raise ValueError("The MPS must be the same length.")
+        self.left, self.right = left, right
+        self.dim = left.dim
+        self.constant = complex(constant) if constant != 0.0 else overlap(left, right)
+
+    def __len__(self):
+        return len(self.left)
+
+    def apply(self, psi):
+        """applyMPO(O, psi): (<left|psi> / constant) * copy(right)."""
+        return self.right * (overlap(self.left, psi) / self.constant)
 
 
 class MPOHandle:

@@ -330,3 +330,59 @@ def test_philox4x32_10_known_answers():
              (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
     for c, k, e in kats:
         assert philox4x32_10(c, k) == e
+
+
+def test_mpo_mps_product_and_vmps_match_dense():
+    """applyMPO (MPOMPSProduct, mpo.jl:125-146) equals the dense operator on
+    the dense state, and vmps (vmps.jl:1-105) fits the dense weighted sum of
+    two MPSs when nothing is truncated."""
+    st = O.spinhalf()
+    N = 6
+    H = xxz(N, 1.0, 0.5)
+    W = O.mpo_from_oplist(st, H)
+    rng = np.random.default_rng(8)
+    psi = O.random_mps(2, N, 3, rng)
+    phi = O.mpo_mps_product(W, psi)
+    ref = X.oplist_to_dense(st, H) @ X.mps_to_dense(psi)
+    assert np.linalg.norm(X.mps_to_dense(phi) - ref) < 1e-10 * np.linalg.norm(ref)
+    assert phi.center == 1
+    p1, p2 = O.random_mps(2, N, 3, rng), O.random_mps(2, N, 2, rng)
+    stats = {}
+    fit = O.vmps(p1, p2, coeffs=[1.0, -0.5j], cutoff=0.0, maxdim=64, stats=stats)
+    target = X.mps_to_dense(p1) - 0.5j * X.mps_to_dense(p2)
+    assert np.linalg.norm(X.mps_to_dense(fit) - target) < 1e-10 * np.linalg.norm(target)
+    assert abs(stats["cost"] + np.vdot(target, target).real) < 1e-9
+    # the projector |p2><p2| / <p2|p2> applied to p1
+    P = O.MPSProjector(p2)
+    v2 = X.mps_to_dense(p2)
+    ref = v2 * np.vdot(v2, X.mps_to_dense(p1)) / np.vdot(v2, v2)
+    assert np.allclose(X.mps_to_dense(P.apply(p1)), ref, atol=1e-12)
+
+
+def test_tebd_with_projector_finds_excited_state():
+    """tebd(...; projectors) (tebd.jl:23-41,67-73): imaginary time with the
+    ground state projected out every step converges to the first excited
+    state of a gapped transverse-field Ising chain.  The all-up start overlaps
+    both parity sectors (a Neel start has no weight on the first excited
+    state); the tolerance covers the O(dt) Trotter bias at dt = 0.05."""
+    st = O.spinhalf()
+    N = 6
+    H = O.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], -1.0)
+    for i in range(1, N + 1):
+        H.add("x", i, -1.5)
+    ev = np.linalg.eigvalsh(X.oplist_to_dense(st, H))
+    W = O.mpo_from_oplist(st, H)
+    g = O.random_mps(2, N, 4, np.random.default_rng(1))
+    g, _ = O.dmrg(g, W, maxdim=32, cutoff=1e-14, minsweeps=8, maxsweeps=8, numconverges=np.inf)
+    mH = O.OpList(N)  # the gates are exp(+dt H'): H' = -H for cooling
+    for ops, sites, c in zip(H.ops, H.sites, H.coeffs):
+        mH.add(ops, sites, -c)
+    psi = O.product_mps(st, ["up"] * N)
+    psi, _ = O.tebd(st, psi, mH, 0.05, 8.0, 8.0, cutoff=1e-12, maxdim=32, projectors=[g],
+                    projection_every=1)
+    v = X.mps_to_dense(psi)
+    v /= np.linalg.norm(v)
+    assert abs(X.dense_expect(v, X.oplist_to_dense(st, H)) - ev[1]) < 2e-5
+    assert abs(np.vdot(X.mps_to_dense(g), v)) < 1e-6
