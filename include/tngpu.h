@@ -277,6 +277,27 @@ int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, in
                       int32_t save_every, int32_t nobs, const int32_t* obs_sites,
                       const double* obs_ops, double* obs_avg, int32_t* njumps_per_traj,
                       int32_t nworkers);
+/* The same ensemble as one persistent device launch: every block of the
+ * launch runs whole trajectories on the device (gates, truncated splits with
+ * a one-block FP64 eigensolver, norm, emission rates, draws, jumps,
+ * observables) with no host round trip per gate, each in a slot of fixed
+ * capacity: trunc->maxdim >= 1 bounds every bond (with the initial state's
+ * bonds), d <= 4, d x bond dimension <= 256, at most 1024 sites, one- and
+ * two-site gates.  Draws as tn_qjmc_batch; with draws == NULL trajectory t
+ * uses the stream tn_philox_uniforms(seed, first_traj + t, ...), unbounded.
+ * jumps/jumptimes (optional, ntraj x max_jumps) receive the 1-based jump
+ * channels and times of each trajectory (max_jumps = 0: none returned, one
+ * per step allowed).  blocks_per_sm (1..8) sets the launch width: blocks =
+ * min(ntraj, SMs x blocks_per_sm).  Replaces the loop of qjmc_simulation
+ * calls (qjmc.jl:28-166) over an ensemble. */
+int32_t tn_qjmc_ensemble(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, int32_t njump,
+                         const int32_t* jump_sites, const double* jump_ops,
+                         const double* jump_coeffs, int32_t nsteps, double dt, int32_t ntraj,
+                         const double* draws, int64_t ndraws_per_traj, uint64_t seed,
+                         uint32_t first_traj, const tn_trunc_opts* trunc, int32_t save_every,
+                         int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
+                         double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
+                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm);
 /* The per-trajectory uniform stream of tn_qjmc_batch: out[k] in [0, 1) is the
  * top 53 bits of 64-bit word k % 2 of Philox4x32-10 (Salmon et al., SC 2011)
  * at counter (k / 2 low 32 bits, trajectory, k / 2 high 32 bits, 0) under the

@@ -35,6 +35,12 @@ void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsi
                 const double* draws, int64_t ndraws_per_traj, uint64_t seed, const Trunc& t,
                 int save_every, int nobs, const int* obs_sites, const double* obs_ops,
                 double* obs_avg, int* njumps_per_traj, int nworkers);
+void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsites,
+                   const double* jops, const double* jcoeffs, int nsteps, double dt, int ntraj,
+                   const double* draws, int64_t ndraws_per_traj, uint64_t seed, uint32_t first_traj,
+                   const Trunc& t, int save_every, int nobs, const int* obs_sites,
+                   const double* obs_ops, double* obs_avg, int* njumps_per_traj, int max_jumps,
+                   int* jumps, double* jumptimes, int blocks_per_sm);
 void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out);
 struct VmpsResult {
     double cost;
@@ -706,6 +712,23 @@ int32_t tn_qjmc_batch(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32_t 
     qjmc_batch(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
                ndraws_per_traj, seed, to_trunc(t), save_every, nobs, obs_sites, obs_ops, obs_avg,
                njumps_per_traj, nworkers);
+    TN_API_END
+}
+
+int32_t tn_qjmc_ensemble(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32_t njump,
+                         const int32_t* jump_sites, const double* jump_ops,
+                         const double* jump_coeffs, int32_t nsteps, double dt, int32_t ntraj,
+                         const double* draws, int64_t ndraws_per_traj, uint64_t seed,
+                         uint32_t first_traj, const tn_trunc_opts* t, int32_t save_every,
+                         int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
+                         double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
+                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(psi0 && g && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
+    TN_REQUIRE(nobs == 0 || (obs_sites && obs_ops), "null observables");
+    qjmc_ensemble(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
+                  ndraws_per_traj, seed, first_traj, to_trunc(t), save_every, nobs, obs_sites,
+                  obs_ops, obs_avg, njumps_per_traj, max_jumps, jumps, jumptimes, blocks_per_sm);
     TN_API_END
 }
 

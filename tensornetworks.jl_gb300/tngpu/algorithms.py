@@ -374,14 +374,22 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
                   draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
-                  seed=None, first_traj=0):
+                  seed=None, first_traj=0, engine="auto", blocks_per_sm=2, records=False):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,
-    averaged single-site observables [rows x terms], jump counts).  ``draws``
-    is an (ntraj x m) array of uniforms consumed per trajectory in the
-    reference's order; with ``seed`` trajectory t draws from its own
+    averaged single-site observables [rows x terms], jump counts), and with
+    ``records`` also the per-trajectory jump channels (1-based) and times.
+    ``draws`` is an (ntraj x m) array of uniforms consumed per trajectory in
+    the reference's order; with ``seed`` trajectory t draws from its own
     counter-based stream philox_uniforms(seed, first_traj + t); otherwise
-    the draws come from ``rand``."""
+    the draws come from ``rand``.
+
+    engine="device" runs the whole ensemble as one persistent launch
+    (tn_qjmc_ensemble: every block runs whole trajectories, ``blocks_per_sm``
+    blocks per SM; needs maxdim >= 1 with d * maxdim <= 256);
+    engine="workers" runs ``workers`` host threads, each driving one
+    trajectory at a time on its own stream (tn_qjmc_batch); "auto" takes the
+    device engine whenever it applies."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -389,11 +397,18 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     gates = GateList(H.length, rows, st.dim, psi.ctx)
     if any(len(s) != 1 for s in jumpops.sites) or any(len(s) != 1 for s in obs.sites):
         raise NotImplementedError("single-site jump operators and observables only")
+    fits = maxdim >= 1 and st.dim <= 4 and st.dim * max(maxdim, max(psi.bonddims())) <= 256
+    if engine == "auto":
+        engine = "device" if fits else "workers"
+    if engine not in ("device", "workers"):
+        raise ValueError("engine must be 'auto', 'device' or 'workers'")
+    if engine == "device" and not fits:
+        raise ValueError("the device engine needs maxdim >= 1, d <= 4 and d * maxdim <= 256")
     if draws is None and seed is None:
         g = rand if rand is not None else np.random.default_rng()
         draws = g.random((ntraj, 3 * steps + 3))
-    if draws is None and first_traj != 0:
-        # the library numbers its streams from 0: draw shifted ones here
+    if draws is None and first_traj != 0 and engine == "workers":
+        # the worker engine numbers its streams from 0: draw shifted ones here
         draws = np.stack([philox_uniforms(seed, first_traj + t, 3 * steps + 3)
                           for t in range(ntraj)])
     if draws is not None:
@@ -414,16 +429,32 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     nj = np.zeros(ntraj, dtype=np.int32)
     t = L.trunc(cutoff, maxdim, mindim)
     ctx = psi.ctx
-    ctx.check(ctx.lib.tn_qjmc_batch(
-        ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
-        L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, C.byref(t), savesteps,
-        len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
-        nj.ctypes.data_as(L.i32p), int(workers)))
+    if engine == "device":
+        mj = steps + 1 if records else 0
+        jch = np.zeros((ntraj, max(mj, 1)), dtype=np.int32)
+        jtm = np.zeros((ntraj, max(mj, 1)))
+        ctx.check(ctx.lib.tn_qjmc_ensemble(
+            ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
+            L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, int(first_traj),
+            C.byref(t), savesteps, len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops),
+            L.as_dp(out), nj.ctypes.data_as(L.i32p), mj, jch.ctypes.data_as(L.i32p),
+            L.as_dp(jtm), int(blocks_per_sm)))
+    else:
+        if records:
+            raise ValueError("jump records come from the device engine")
+        ctx.check(ctx.lib.tn_qjmc_batch(
+            ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
+            L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, C.byref(t), savesteps,
+            len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
+            nj.ctypes.data_as(L.i32p), int(workers)))
     tt, times = 0.0, [0.0]
     for i in range(1, steps + 1):
         tt += dt
         if i % savesteps == 0:
             times.append(tt)
+    if records:
+        return (times, out, nj, [list(jch[r, :nj[r]]) for r in range(ntraj)],
+                [list(jtm[r, :nj[r]]) for r in range(ntraj)])
     return times, out, nj
 
 

@@ -429,7 +429,7 @@ def test_qjmc_ensemble_matches_per_trajectory_oracle(tn, workers, ntraj):
     pg = tn.productMPS(tn.spinhalf(), ["up"] * N)
     times, out, nj = tn.qjmc_ensemble(tn.spinhalf(), pg, Hg, Lg, steps * dt, dt, zg, ntraj,
                                       draws=draws, save=5 * dt, cutoff=1e-10, maxdim=16,
-                                      workers=workers)
+                                      workers=workers, engine="workers")
     assert list(nj) == counts and sum(counts) > 0
     assert out.shape == avg.shape and np.allclose(np.real(out), avg, atol=1e-9)
     assert len(times) == out.shape[0]

@@ -1,0 +1,106 @@
+"""The persistent trajectory engine (tn_qjmc_ensemble): every block of one
+launch runs whole quantum-jump trajectories (qjmc.jl:28-220) on the device.
+
+  * Against the oracle's qjmc_simulation run trajectory by trajectory on the
+    same explicit uniform streams: identical jump channels and times in
+    every trajectory, and the trajectory-averaged <Z_i>(t) to 1e-9 (chains
+    with an even and an odd number of sites: the odd one puts one-site gates
+    at the chain's end).
+  * Against the host-worker engine (tn_qjmc_batch) on the same seeded
+    streams: identical jump counts, averaged <Z_i>(t) to 1e-9.
+  * The launch width (blocks per SM) does not change any trajectory.
+  * A draw stream that runs out is reported as an error status."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tn():
+    import tngpu
+    return tngpu
+
+
+def _model(mod, N, g=0.5, h=0.8):
+    H, Lj, Z = mod.OpList(N), mod.OpList(N), mod.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], 1.0)
+    for i in range(1, N + 1):
+        H.add("x", i, h)
+        Lj.add("s-", i, np.sqrt(g))
+        Z.add("z", i)
+    return H, Lj, Z
+
+
+@pytest.mark.parametrize("N", [6, 7])
+def test_engine_jump_records_match_oracle(tn, N):
+    dt, steps, ntraj, every = 0.05, 30, 8, 5
+    draws = np.random.default_rng(40 + N).random((ntraj, 3 * steps + 3))
+    Ho, Lo, Zo = _model(O, N)
+    avg, jumps, times = 0.0, [], []
+    for t in range(ntraj):
+        po = O.product_mps(O.spinhalf(), ["up"] * N)
+        rec = {}
+        j, jt = O.qjmc_simulation(O.spinhalf(), po, Ho, Lo, steps * dt, dt,
+                                  O.algorithms.UniformStream(draws[t]), [Zo], save=every * dt,
+                                  cutoff=1e-10, maxdim=16, record=rec)
+        avg = avg + np.real(np.array([r[0] for r in rec["ops"]]))
+        jumps.append(list(j))
+        times.append(list(jt))
+    avg /= ntraj
+    Hg, Lg, Zg = _model(tn, N)
+    st = tn.spinhalf()
+    pg = tn.productMPS(st, ["up"] * N)
+    tg, out, nj, jg, jtg = tn.qjmc_ensemble(st, pg, Hg, Lg, steps * dt, dt, Zg, ntraj, draws=draws,
+                                            save=every * dt, cutoff=1e-10, maxdim=16,
+                                            engine="device", records=True)
+    assert sum(len(j) for j in jumps) > ntraj  # the stream exercises the jump branch
+    assert [list(map(int, j)) for j in jg] == jumps
+    for a, b in zip(jtg, times):
+        assert np.allclose(a, b, rtol=0, atol=1e-12)
+    assert list(nj) == [len(j) for j in jumps]
+    assert out.shape == avg.shape and np.allclose(np.real(out), avg, atol=1e-9)
+    assert len(tg) == out.shape[0]
+
+
+def test_engine_matches_worker_engine_seeded(tn):
+    N, dt, steps, ntraj = 10, 0.02, 60, 16
+    H, Lj, Z = _model(tn, N)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up"] * N)
+    kw = dict(cutoff=1e-10, maxdim=32, seed=5, save=10 * dt)
+    _, za, na = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, engine="workers",
+                                 workers=8, **kw)
+    _, zb, nb = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, engine="device", **kw)
+    assert na.tolist() == nb.tolist() and na.sum() > 0
+    assert np.allclose(za, zb, atol=1e-9)
+
+
+def test_engine_launch_width_invariance(tn):
+    N, dt, steps, ntraj = 8, 0.05, 20, 12
+    H, Lj, Z = _model(tn, N)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up"] * N)
+    res = [tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, seed=3, cutoff=1e-10,
+                            maxdim=16, engine="device", blocks_per_sm=b, records=True)
+           for b in (1, 4)]
+    assert np.array_equal(res[0][1], res[1][1])
+    assert res[0][3] == res[1][3] and res[0][4] == res[1][4]
+
+
+def test_engine_reports_an_exhausted_stream(tn):
+    N, dt, steps = 6, 0.05, 10
+    H, Lj, Z = _model(tn, N)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up"] * N)
+    draws = np.full((2, 5), 0.5)  # two per step are needed: the third step runs out
+    with pytest.raises(tn.TNError, match="exhausted"):
+        tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 2, draws=draws, cutoff=1e-10,
+                         maxdim=16, engine="device")
+    with pytest.raises(ValueError, match="maxdim"):
+        tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 2, draws=draws, cutoff=1e-10,
+                         maxdim=0, engine="device")

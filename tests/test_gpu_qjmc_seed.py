@@ -1,4 +1,4 @@
-"""Seeded QJMC ensembles (tn_qjmc_batch with draws == NULL): trajectory t
+"""Seeded QJMC ensembles (tn_qjmc_batch and tn_qjmc_ensemble with draws == NULL): trajectory t
 draws from its own Philox4x32-10 stream, so the ensemble equals the one run
 from the same streams passed explicitly (the parity mode), and a block of
 trajectories started at first_traj equals the matching rows of the full
@@ -21,13 +21,14 @@ def _model(tn, N):
     return H, Lj, Z
 
 
-def test_seeded_ensemble_matches_explicit_streams():
+@pytest.mark.parametrize("engine", ["workers", "device"])
+def test_seeded_ensemble_matches_explicit_streams(engine):
     import tngpu as tn
     N, dt, steps, ntraj = 8, 0.05, 30, 6
     H, Lj, Z = _model(tn, N)
     st = tn.spinhalf()
     psi = tn.productMPS(st, ["up"] * N)
-    kw = dict(cutoff=1e-10, maxdim=16, workers=3)
+    kw = dict(cutoff=1e-10, maxdim=16, workers=3, engine=engine)
     _, za, na = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, seed=11, **kw)
     draws = np.stack([tn.philox_uniforms(11, t, 3 * steps + 3) for t in range(ntraj)])
     _, zb, nb = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, draws=draws, **kw)
