@@ -288,8 +288,12 @@ int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, in
  * jumps/jumptimes (optional, ntraj x max_jumps) receive the 1-based jump
  * channels and times of each trajectory (max_jumps = 0: none returned, one
  * per step allowed).  blocks_per_sm (1..8) sets the launch width: blocks =
- * min(ntraj, SMs x blocks_per_sm).  Replaces the loop of qjmc_simulation
- * calls (qjmc.jl:28-166) over an ensemble. */
+ * min(ntraj, SMs x blocks_per_sm).  stats (optional, 4 values): the
+ * algorithmic FP64 flops of all trajectories (contractions, Gram products,
+ * the LAPACK count 16/3 n^3 + 8 n^2 k of each eigensolve), the launch's
+ * device time in ms (CUDA events on the context's stream), the
+ * trajectory-steps and the blocks launched.  Replaces the loop of
+ * qjmc_simulation calls (qjmc.jl:28-166) over an ensemble. */
 int32_t tn_qjmc_ensemble(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, int32_t njump,
                          const int32_t* jump_sites, const double* jump_ops,
                          const double* jump_coeffs, int32_t nsteps, double dt, int32_t ntraj,
@@ -297,7 +301,8 @@ int32_t tn_qjmc_ensemble(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates,
                          uint32_t first_traj, const tn_trunc_opts* trunc, int32_t save_every,
                          int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
                          double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
-                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm);
+                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm,
+                         double* stats);
 /* The per-trajectory uniform stream of tn_qjmc_batch: out[k] in [0, 1) is the
  * top 53 bits of 64-bit word k % 2 of Philox4x32-10 (Salmon et al., SC 2011)
  * at counter (k / 2 low 32 bits, trajectory, k / 2 high 32 bits, 0) under the

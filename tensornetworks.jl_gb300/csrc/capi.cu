@@ -40,7 +40,7 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
                    const double* draws, int64_t ndraws_per_traj, uint64_t seed, uint32_t first_traj,
                    const Trunc& t, int save_every, int nobs, const int* obs_sites,
                    const double* obs_ops, double* obs_avg, int* njumps_per_traj, int max_jumps,
-                   int* jumps, double* jumptimes, int blocks_per_sm);
+                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats);
 void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out);
 struct VmpsResult {
     double cost;
@@ -722,13 +722,15 @@ int32_t tn_qjmc_ensemble(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32
                          uint32_t first_traj, const tn_trunc_opts* t, int32_t save_every,
                          int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
                          double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
-                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm) {
+                         int32_t* jumps, double* jumptimes, int32_t blocks_per_sm,
+                         double* stats) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(psi0 && g && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
     TN_REQUIRE(nobs == 0 || (obs_sites && obs_ops), "null observables");
     qjmc_ensemble(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
                   ndraws_per_traj, seed, first_traj, to_trunc(t), save_every, nobs, obs_sites,
-                  obs_ops, obs_avg, njumps_per_traj, max_jumps, jumps, jumptimes, blocks_per_sm);
+                  obs_ops, obs_avg, njumps_per_traj, max_jumps, jumps, jumptimes, blocks_per_sm,
+                  stats);
     TN_API_END
 }
 

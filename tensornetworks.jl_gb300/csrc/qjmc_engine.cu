@@ -76,6 +76,7 @@ struct QjParams {
     double* jump_time;  // ntraj x maxj
     int* err;           // ntraj status words
     int64_t* used;      // ntraj draws consumed
+    double* flops;      // ntraj algorithmic FP64 flops
 };
 
 // ---- a slot's scratch -----------------------------------------------------------
@@ -159,6 +160,7 @@ struct Traj {
     uint32_t trajno;  // Philox stream number
     int t;            // trajectory index within the launch
     TruncD tr;
+    double fl;  // algorithmic FP64 flops so far (the same in every thread)
     __device__ cplx* A(int i) const { return mps + p->cap_off[i - 1]; }
     __device__ int dl(int i) const { return sh->dims[i - 1]; }
     __device__ int dr(int i) const { return sh->dims[i]; }
@@ -525,12 +527,14 @@ __device__ __noinline__ int split_blk(Traj& T, const cplx* th, int m, int n, boo
     Sh& sh = *T.sh;
     const int g = left_iso ? m : n, sz = min(m, n);
     bgram(left_iso, m, n, th, s.G);
+    T.fl += 4.0 * g * (g + 1) * (double)(left_iso ? n : m);  // lower triangle
     double trace = 0.0;
     for (int i = threadIdx.x; i < g; i += QT) trace += s.G[i + (size_t)g * i].x;
     trace = block_sum(trace, sh.ws);
     const int maxd = (tr.maxdim <= 0 || tr.maxdim > sz) ? sz : tr.maxdim;
     const int want = min(sz, max(maxd, tr.mindim));
     eig_blk(T, s.G, g, want);
+    T.fl += 16.0 / 3.0 * g * g * (double)g + 8.0 * g * g * (double)want;  // LAPACK count
     const int k = keep_blk(s.lama, want, trace, tr, sh);
     if (k > kcap) {
         set_flag(sh, QE_CAPACITY);
@@ -539,8 +543,10 @@ __device__ __noinline__ int split_blk(Traj& T, const cplx* th, int m, int n, boo
     if (left_iso) {  // X = V_k, Y = V_k^H th
         for (int e = threadIdx.x; e < m * k; e += QT) Xo[e] = s.V[e];
         bgemm<OC, ON>(k, n, m, s.V, m, th, m, Yo, k);
+        T.fl += 8.0 * k * n * (double)m;
     } else {  // X = th V_k, Y = V_k^H
         bgemm<ON, ON>(m, k, n, th, m, s.V, n, Xo, m);
+        T.fl += 8.0 * m * k * (double)n;
         for (int e = threadIdx.x; e < k * n; e += QT) {
             const int r = e % k, c = e / k;
             Yo[r + k * c] = cconj(s.V[c + (size_t)n * r]);
@@ -559,6 +565,7 @@ __device__ __noinline__ void moveright(Traj& T, int idx, const TruncD& tr) {
     const int k = split_blk(T, T.s.th, Dl * d, Dr, true, tr, T.A(idx), T.s.tmp, p.cap[idx]);
     if (k < 0) return;
     bgemm<ON, ON>(k, d * Dr2, Dr, T.s.tmp, k, T.A(idx + 1), Dr, T.s.th2, k);
+    T.fl += 8.0 * k * d * Dr2 * (double)Dr;
     bcopy(T.A(idx + 1), T.s.th2, k * d * Dr2);
     if (threadIdx.x == 0) T.sh->dims[idx] = k;
     __syncthreads();
@@ -572,6 +579,7 @@ __device__ __noinline__ void moveleft(Traj& T, int idx, const TruncD& tr) {
     const int k = split_blk(T, T.s.th, Dl, d * Dr, false, tr, T.s.tmp, T.A(idx), p.cap[idx - 1]);
     if (k < 0) return;
     bgemm<ON, ON>(Dl0 * d, k, Dl, T.A(idx - 1), Dl0 * d, T.s.tmp, Dl, T.s.th2, Dl0 * d);
+    T.fl += 8.0 * Dl0 * d * k * (double)Dl;
     bcopy(T.A(idx - 1), T.s.th2, Dl0 * d * k);
     if (threadIdx.x == 0) T.sh->dims[idx - 1] = k;
     __syncthreads();
@@ -599,6 +607,7 @@ __device__ __noinline__ void gate2(Traj& T, int site, const cplx* M, bool direct
     const int d = p.d, d2 = d * d, Dl = T.dl(site), Dm = T.dr(site), Dr = T.dr(site + 1);
     bgemm<ON, ON>(Dl * d, d * Dr, Dm, T.A(site), Dl * d, T.A(site + 1), Dm, T.s.th, Dl * d);
     bapply(T.s.th, T.s.th2, M, d2, d2, Dl, Dr);
+    T.fl += 8.0 * Dl * d * d * (double)Dr * Dm + 8.0 * Dl * Dr * (double)d2 * d2;
     const int k = split_blk(T, T.s.th2, Dl * d, d * Dr, !direction, tr, T.A(site), T.A(site + 1),
                             p.cap[site]);
     if (k < 0) return;
@@ -612,6 +621,7 @@ __device__ __noinline__ void gate2(Traj& T, int site, const cplx* M, bool direct
 __device__ void site_op(Traj& T, int site, const cplx* M) {
     const int d = T.p->d, Dl = T.dl(site), Dr = T.dr(site);
     bapply(T.A(site), T.s.tmp, M, d, d, Dl, Dr);
+    T.fl += 8.0 * Dl * Dr * (double)d * d;
     bcopy(T.A(site), T.s.tmp, Dl * d * Dr);
 }
 
@@ -728,8 +738,10 @@ __device__ __noinline__ void rho_all(Traj& T) {
         const int Dl = T.dl(i), Dr = T.dr(i);
         bgemm<ON, ON>(Dl, d * Dr, Dl, B, Dl, T.A(i), Dl, Y, Dl);
         rho_contract(T.A(i), Y, Dl, d, Dr, T.s.rho + (size_t)(i - 1) * d * d, sh);
+        T.fl += 8.0 * Dl * Dl * (double)d * Dr + 8.0 * Dl * Dr * (double)d * d;
         if (i < N) {
             bgemm<OC, ON>(Dr, Dr, Dl * d, T.A(i), Dl * d, Y, Dl * d, Bn, Dr);
+            T.fl += 8.0 * Dr * Dr * (double)Dl * d;
             cplx* t = B;
             B = Bn;
             Bn = t;
@@ -743,9 +755,14 @@ __device__ __noinline__ void rho_all(Traj& T) {
     for (int i = c; i >= 1; --i) {
         const int Dl = T.dl(i), Dr = T.dr(i);
         bgemm<ON, OT>(Dl * d, Dr, Dr, T.A(i), Dl * d, B, Dr, Y, Dl * d);
-        if (i < c) rho_contract(T.A(i), Y, Dl, d, Dr, T.s.rho + (size_t)(i - 1) * d * d, sh);
+        T.fl += 8.0 * Dl * d * Dr * (double)Dr;
+        if (i < c) {
+            rho_contract(T.A(i), Y, Dl, d, Dr, T.s.rho + (size_t)(i - 1) * d * d, sh);
+            T.fl += 8.0 * Dl * Dr * (double)d * d;
+        }
         if (i > 1) {
             bgemm<OR, OT>(Dl, Dl, d * Dr, T.A(i), Dl, Y, Dl, Bn, Dl);
+            T.fl += 8.0 * Dl * Dl * (double)d * Dr;
             cplx* t = B;
             B = Bn;
             Bn = t;
@@ -792,6 +809,7 @@ __device__ void run_traj(const QjParams& p, Sh& sh, int t, int slot) {
     T.trajno = p.first_traj + (uint32_t)t;
     T.t = t;
     T.tr = TruncD{p.cutoff, p.maxdim, p.mindim};
+    T.fl = 0.0;
     const int N = p.N, d = p.d;
     for (int i = 1; i <= N; ++i) {
         const int n = p.psi0_dims[i - 1] * d * p.psi0_dims[i];
@@ -878,6 +896,7 @@ __device__ void run_traj(const QjParams& p, Sh& sh, int t, int slot) {
         p.err[t] = sh.flag;
         p.njumps[t] = nj;
         p.used[t] = (int64_t)T.used;
+        p.flops[t] = T.fl;
     }
     __syncthreads();
 }
@@ -931,7 +950,7 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
                    const double* draws, int64_t ndraws_per_traj, uint64_t seed, uint32_t first_traj,
                    const Trunc& t, int save_every, int nobs, const int* obs_sites,
                    const double* obs_ops, double* obs_avg, int* njumps_per_traj, int max_jumps,
-                   int* jumps, double* jumptimes, int blocks_per_sm) {
+                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats) {
     Ctx* ctx = psi0->ctx;
     const int N = psi0->N, d = psi0->d;
     TN_REQUIRE(g->N == N && g->d == d, "GateList and MPS do not match.");
@@ -1032,7 +1051,7 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
     DBuf obs_traj(ctx, sizeof(cplx) * (size_t)ntraj * nrows_out * std::max(nobs, 1));
     DBuf d_nj(ctx, sizeof(int) * ntraj), d_jc(ctx, sizeof(int) * (size_t)ntraj * maxj),
         d_jt(ctx, sizeof(double) * (size_t)ntraj * maxj), d_err(ctx, sizeof(int) * ntraj),
-        d_used(ctx, sizeof(int64_t) * ntraj), d_avg(ctx, sizeof(cplx) * (size_t)nrows_out * std::max(nobs, 1));
+        d_used(ctx, sizeof(int64_t) * ntraj), d_fl(ctx, sizeof(double) * ntraj), d_avg(ctx, sizeof(cplx) * (size_t)nrows_out * std::max(nobs, 1));
 
     QjParams p{};
     p.N = N;
@@ -1080,9 +1099,13 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
     p.jump_time = d_jt.d();
     p.err = d_err.as<int>();
     p.used = d_used.as<int64_t>();
+    p.flops = d_fl.d();
+    cudaEvent_t e0 = ctx->ev_get(), e1 = ctx->ev_get();
+    TN_CHECK_CUDA(cudaEventRecord(e0, ctx->stream));
     qjmc_engine_kernel<<<slots, QT, 0, ctx->stream>>>(p);
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
+    TN_CHECK_CUDA(cudaEventRecord(e1, ctx->stream));
     if (nobs > 0 && nrows_out > 1) {
         const int n = (nrows_out - 1) * nobs;
         obs_reduce_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(obs_traj.c(), ntraj, nrows_out,
@@ -1105,7 +1128,22 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
     if (jumptimes && max_jumps > 0)
         TN_CHECK_CUDA(cudaMemcpyAsync(jumptimes, d_jt.p, sizeof(double) * (size_t)ntraj * max_jumps,
                                       cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> fl(ntraj);
+    TN_CHECK_CUDA(cudaMemcpyAsync(fl.data(), d_fl.p, sizeof(double) * ntraj, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
     ctx->sync();
+    float ms = 0.f;
+    TN_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    ctx->ev_pool.push_back(e0);
+    ctx->ev_pool.push_back(e1);
+    if (stats) {
+        double f = 0.0;
+        for (double v : fl) f += v;
+        stats[0] = f;
+        stats[1] = ms;
+        stats[2] = (double)ntraj * nsteps;
+        stats[3] = slots;
+    }
     for (int i = 0; i < ntraj; ++i) {
         switch (err[i]) {
             case QE_OK: break;

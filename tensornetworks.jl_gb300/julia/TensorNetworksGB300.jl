@@ -21,6 +21,8 @@ const libtngpu = get(ENV, "TNGPU_LIB", joinpath(@__DIR__, "..", "tngpu", "libtng
 
 const TN_PREC_FP64 = Int32(0)
 const TN_PREC_MIXED = Int32(1)
+const TN_PREC_MIXED_ENV64 = Int32(2)
+prec_code(p::Symbol) = p === :mixed ? TN_PREC_MIXED : p === :mixed_env64 ? TN_PREC_MIXED_ENV64 : TN_PREC_FP64
 
 struct TruncOpts
     cutoff::Float64
@@ -149,7 +151,7 @@ function dmrg(psi::GMPS, H::GMPS; nsites::Int=2, krylovdim::Int=3, kryloviter::I
     hH = upload_mpo(ctx, H)
     opts = DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
                     Float64(numconverges), cutoff, maxdim, mindim,
-                    precision === :mixed ? TN_PREC_MIXED : TN_PREC_FP64, verbose, 0, -1)
+                    prec_code(precision), verbose, 0, -1)
     energy = Ref{Float64}(0.0)
     stats = Ref(DmrgStats())
     try
@@ -162,6 +164,115 @@ function dmrg(psi::GMPS, H::GMPS; nsites::Int=2, krylovdim::Int=3, kryloviter::I
         ccall((:tn_mpo_destroy, libtngpu), Int32, (Ptr{Cvoid},), hH)
     end
     return psi, energy[]
+end
+
+# dmrg(psi, Hs::GMPS...; coeffs) over a sum of terms (dmrg.jl:128-154,
+# projmpssum.jl): rank-2 terms are MPOs, rank-1 terms MPS projectors
+# coeff |phi><phi| (ProjMPS(phi, psi; squared=true)).
+function dmrg(psi::GMPS, Hs::GMPS...; coeffs=ones(length(Hs)), nsites::Int=2,
+              krylovdim::Int=3, kryloviter::Int=2, minsweeps::Int=1, maxsweeps::Int=1000,
+              tol::Float64=1e-10, tolgrad::Float64=1e-5, numconverges::Real=4,
+              cutoff::Float64=1e-12, maxdim::Int=1000, mindim::Int=1, verbose::Bool=true,
+              precision::Symbol=:fp64, kwargs...)
+    length(Hs) == 1 && rank(Hs[1]) == 2 && coeffs == [1] &&
+        return dmrg(psi, Hs[1]; nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol,
+                    tolgrad, numconverges, cutoff, maxdim, mindim, verbose, precision)
+    ctx = context()
+    hpsi = upload(ctx, psi)
+    mpos = Ptr{Cvoid}[]; mc = Float64[]; projs = Ptr{Cvoid}[]; pc = Float64[]
+    try
+        for (H, c) in zip(Hs, coeffs)
+            if rank(H) == 2
+                push!(mpos, upload_mpo(ctx, H)); push!(mc, Float64(c))
+            else
+                push!(projs, upload(ctx, H)); push!(pc, Float64(c))
+            end
+        end
+        opts = DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
+                        Float64(numconverges), cutoff, maxdim, mindim, prec_code(precision),
+                        verbose, 0, -1)
+        energy = Ref{Float64}(0.0)
+        stats = Ref(DmrgStats())
+        check(ctx, ccall((:tn_dmrg_sum, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Float64}, Int32,
+                          Ptr{Ptr{Cvoid}}, Ptr{Float64}, Ref{DmrgOpts}, Ref{Float64}, Ref{DmrgStats}),
+                         ctx.h, hpsi, length(mpos), mpos, mc, length(projs), projs, pc, opts,
+                         energy, stats))
+        download!(ctx, psi, hpsi)
+        return psi, energy[]
+    finally
+        destroy_mps(hpsi)
+        foreach(h -> ccall((:tn_mpo_destroy, libtngpu), Int32, (Ptr{Cvoid},), h), mpos)
+        foreach(destroy_mps, projs)
+    end
+end
+
+# ---- vmps, applyMPO, inner (vmps.jl:1-105, mpo.jl:105-250) ---------------------
+struct VmpsOpts
+    nsites::Int32
+    minsweeps::Int32
+    maxsweeps::Int32
+    tol::Float64
+    numconverges::Float64
+    cutoff::Float64
+    maxdim::Int64
+    mindim::Int64
+    verbose::Int32
+end
+
+function new_gmps(ctx::Context, h::Ptr{Cvoid}, like::GMPS)
+    out = GMPS(1, dim(like), [zeros(ComplexF64, 1, dim(like), 1) for _ in 1:length(like)], 0)
+    download!(ctx, out, h)
+    destroy_mps(h)
+    return out
+end
+
+function vmps(psis::GMPS...; coeffs=ones(length(psis)), nsites::Int=2, minsweeps::Int=2,
+              maxsweeps::Int=200, tol::Real=1e-10, numconverges::Real=3, cutoff::Real=1e-12,
+              maxdim::Int=1000, mindim::Int=1, verbose::Bool=false, kwargs...)
+    ctx = context()
+    hs = [upload(ctx, p) for p in psis]
+    cs = ComplexF64.(coeffs)
+    out = Ref{Ptr{Cvoid}}(C_NULL); cost = Ref{Float64}(0.0); sw = Ref{Int32}(0)
+    try
+        check(ctx, ccall((:tn_vmps, libtngpu), Int32,
+                         (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{ComplexF64}, Ref{VmpsOpts},
+                          Ref{Ptr{Cvoid}}, Ref{Float64}, Ref{Int32}),
+                         ctx.h, length(hs), hs, cs,
+                         VmpsOpts(nsites, minsweeps, maxsweeps, tol, numconverges, cutoff, maxdim,
+                                  mindim, verbose), out, cost, sw))
+        return new_gmps(ctx, out[], psis[1])
+    finally
+        foreach(destroy_mps, hs)
+    end
+end
+
+function applyMPO(O::GMPS, psi::GMPS; cutoff::Real=0.0, maxdim::Int=0, mindim::Int=1, kwargs...)
+    ctx = context()
+    hO = upload_mpo(ctx, O); hp = upload(ctx, psi)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    try
+        check(ctx, ccall((:tn_mpo_apply, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{TruncOpts}, Ref{Ptr{Cvoid}}),
+                         ctx.h, hO, hp, TruncOpts(cutoff, maxdim, mindim), out))
+        return new_gmps(ctx, out[], psi)
+    finally
+        ccall((:tn_mpo_destroy, libtngpu), Int32, (Ptr{Cvoid},), hO)
+        destroy_mps(hp)
+    end
+end
+
+function inner(phi::GMPS, psi::GMPS)
+    ctx = context()
+    ha = upload(ctx, phi); hb = upload(ctx, psi)
+    v = zeros(Float64, 2)
+    try
+        check(ctx, ccall((:tn_mps_overlap, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}), ctx.h, ha, hb, v))
+        return complex(v[1], v[2])
+    finally
+        destroy_mps(ha); destroy_mps(hb)
+    end
 end
 
 # ---- gates, applygates!, tebd (gatelist.jl:191-227, tebd.jl:3-100) -----------
@@ -280,6 +391,46 @@ function qjmc_simulation(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, t
         ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
     end
     return Int.(jumps[1:nj[]]), jtimes[1:nj[]]
+end
+
+# An ensemble of ntraj trajectories of qjmc_simulation in one persistent
+# launch (tn_qjmc_ensemble); trajectory t draws from the Philox stream
+# (seed, first_traj + t).  Returns the save times, the trajectory-averaged
+# single-site observables and the jump counts.
+function qjmc_ensemble(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, tmax::Real, dt::Real,
+                       obs::OpList, ntraj::Integer; seed::Integer=0, first_traj::Integer=0,
+                       save::Real=0, cutoff::Real=1e-12, mindim::Int=1, maxdim::Int=64,
+                       blocks_per_sm::Integer=2)
+    save = save == 0 ? dt : save
+    steps = Int(ceil(round(tmax / dt, digits=5)))
+    savesteps = Int(ceil(round(save / dt)))
+    escapeops, gates = TensorNetworks.qjmc_gates(st, H, jumpops, dt)
+    ctx = context()
+    hpsi = upload(ctx, psi)
+    hg = upload_gates(ctx, gates, dim(psi))
+    jsites = Int32[s[1] for s in jumpops.sites]
+    jops = reduce(vcat, [vec(op(st, o[1])) for o in jumpops.ops])
+    jco = ComplexF64.(jumpops.coeffs)
+    osites = Int32[s[1] for s in obs.sites]
+    oops = reduce(vcat, [vec(c * op(st, o[1])) for (o, c) in zip(obs.ops, obs.coeffs)])
+    nrows = steps ÷ savesteps + 1
+    avg = zeros(ComplexF64, length(osites), nrows)   # row-major rows x terms in C order
+    nj = zeros(Int32, ntraj)
+    try
+        check(ctx, ccall((:tn_qjmc_ensemble, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{ComplexF64},
+                          Ptr{ComplexF64}, Int32, Float64, Int32, Ptr{Float64}, Int64, UInt64, UInt32,
+                          Ref{TruncOpts}, Int32, Int32, Ptr{Int32}, Ptr{ComplexF64}, Ptr{ComplexF64},
+                          Ptr{Int32}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}),
+                         ctx.h, hpsi, hg, length(jsites), jsites, jops, jco, steps, dt, ntraj,
+                         C_NULL, 0, UInt64(seed), UInt32(first_traj),
+                         TruncOpts(cutoff, maxdim, mindim), savesteps, length(osites), osites,
+                         oops, avg, nj, 0, C_NULL, C_NULL, blocks_per_sm, C_NULL))
+    finally
+        destroy_mps(hpsi)
+        ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)
+    end
+    return collect(0:savesteps:steps) .* dt, permutedims(avg), Int.(nj)
 end
 
 # ---- differentiated TEBD: value and gradient for an rrule ---------------------

@@ -374,7 +374,8 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
                   draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
-                  seed=None, first_traj=0, engine="auto", blocks_per_sm=2, records=False):
+                  seed=None, first_traj=0, engine="auto", blocks_per_sm=2, records=False,
+                  stats=None):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,
     averaged single-site observables [rows x terms], jump counts), and with
@@ -389,7 +390,9 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     blocks per SM; needs maxdim >= 1 with d * maxdim <= 256);
     engine="workers" runs ``workers`` host threads, each driving one
     trajectory at a time on its own stream (tn_qjmc_batch); "auto" takes the
-    device engine whenever it applies."""
+    device engine whenever it applies.  ``stats`` (a dict) receives the
+    device engine's algorithmic FP64 flops, launch time (CUDA events) and
+    trajectory-steps."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -433,12 +436,16 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
         mj = steps + 1 if records else 0
         jch = np.zeros((ntraj, max(mj, 1)), dtype=np.int32)
         jtm = np.zeros((ntraj, max(mj, 1)))
+        sb = np.zeros(4)
         ctx.check(ctx.lib.tn_qjmc_ensemble(
             ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
             L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, int(first_traj),
             C.byref(t), savesteps, len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops),
             L.as_dp(out), nj.ctypes.data_as(L.i32p), mj, jch.ctypes.data_as(L.i32p),
-            L.as_dp(jtm), int(blocks_per_sm)))
+            L.as_dp(jtm), int(blocks_per_sm), L.as_dp(sb)))
+        if stats is not None:
+            stats.update(flops=float(sb[0]), kernel_ms=float(sb[1]), traj_steps=float(sb[2]),
+                         blocks=int(sb[3]))
     else:
         if records:
             raise ValueError("jump records come from the device engine")
