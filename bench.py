@@ -392,43 +392,36 @@ def accuracy_arms(tn, psi, W_mpo, kw, modes=("mixed", "mixed-env64")):
     return out
 
 
-def qjmc_sample(tn, ctx, pre_steps=100, steps=20, ntraj=256, workers=64):
-    """QJMC workload shapes: N=32 Ising chain H = sum Z Z + 0.8 sum X, jumps
-    L_i = sqrt(0.1) s-_i, all-up start, dt=0.01, maxdim 64, cutoff 1e-10.  One
-    trajectory is evolved `pre_steps` (untimed) so the timed steps run at grown
-    bond dimension; from it, `steps` steps of one trajectory alone and of
-    `ntraj` trajectories on `workers` concurrent streams are timed."""
-    N, dt = 32, 0.01
-    H, Lj, Z = tn.OpList(N), tn.OpList(N), tn.OpList(N)
-    for i in range(1, N):
-        H.add(["z", "z"], [i, i + 1], 1.0)
-    for i in range(1, N + 1):
-        H.add("x", i, 0.8)
-        Lj.add("s-", i, np.sqrt(0.1))
-        Z.add("z", i)
+def qjmc_sample(tn, ctx, steps=200, ntraj=304):
+    """Batched-QJMC sample on the DMRG line: the workload of --workload qjmc
+    (N=32 Ising chain, L_i = sqrt(0.1) s-_i, all-up, dt=0.01, maxdim 64,
+    cutoff 1e-10, Philox seed 2024) for `steps` steps: `ntraj` trajectories
+    in one persistent engine launch against trajectory 0 alone through the
+    single-trajectory driver on the same stream."""
+    N, dt, seed = 32, 0.01, 2024
+    H, Lj, Z = qjmc_model(tn, N)
     st = tn.spinhalf()
     psi = tn.productMPS(st, ["up"] * N, ctx=ctx)
-    rng = np.random.default_rng(4)
+    kw = dict(cutoff=1e-10, maxdim=64, save=10 * dt)
+    tn.qjmc_ensemble(st, psi, H, Lj, 2 * dt, dt, Z, 8, seed=seed, engine="device", **kw)
+    stt = {}
     t0 = time.perf_counter()
-    tn.qjmc_simulation(st, psi, H, Lj, pre_steps * dt, dt, [], cutoff=1e-10, maxdim=64,
-                       draws=rng.random(3 * pre_steps + 3))
-    pre_s = time.perf_counter() - t0
-    chi = psi.maxbonddim()
-    seeds = np.random.SeedSequence(4).spawn(ntraj)
-    draws = np.stack([np.random.default_rng(s).random(3 * steps + 3) for s in seeds])
-    t0 = time.perf_counter()
-    tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 1, draws=draws[:1], cutoff=1e-10,
-                     maxdim=64, workers=1)
-    single = steps / (time.perf_counter() - t0)
-    t0 = time.perf_counter()
-    _, zav, nj = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, draws=draws,
-                                  cutoff=1e-10, maxdim=64, workers=workers)
+    _, zav, nj = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, seed=seed,
+                                  engine="device", stats=stt, **kw)
     batched = ntraj * steps / (time.perf_counter() - t0)
+    draws = tn.philox_uniforms(seed, 0, 3 * steps + 3)[None, :]
+    t0 = time.perf_counter()
+    _, _, n1 = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 1, draws=draws,
+                                engine="workers", workers=1, **kw)
+    single = steps / (time.perf_counter() - t0)
     return {"traj_steps_per_s_single": single, "traj_steps_per_s_batched": batched,
-            "batched_vs_single": batched / single, "start_chi": chi, "pre_steps_s": pre_s,
-            "jumps_in_sample": int(nj.sum()), "z_avg_final": float(np.real(zav[-1]).mean()),
-            "sample": f"{ntraj} trajectories x {steps} steps on {workers} streams vs 1 x {steps}, "
-                      f"from a state evolved {pre_steps} steps (chi {chi}); N=32, dt=0.01, maxdim 64"}
+            "batched_vs_single": batched / single, "jumps_traj0": {"engine": int(nj[0]),
+                                                                   "single": int(n1[0])},
+            "engine_fp64_tflops": stt["flops"] / (stt["kernel_ms"] * 1e-3) / 1e12,
+            "z_avg_final": float(np.real(zav[-1]).mean()),
+            "sample": f"{ntraj} trajectories x {steps} steps in one engine launch vs trajectory 0 "
+                      f"alone through the single-trajectory driver; N=32, dt=0.01, maxdim 64, "
+                      f"from the all-up state (the full run is --workload qjmc)"}
 
 
 def tebd_sample(tn, ctx, pre_steps=20, steps=4):

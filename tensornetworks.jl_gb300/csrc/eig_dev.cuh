@@ -99,13 +99,17 @@ __device__ __forceinline__ cplx refl(const cplx* __restrict__ A, int64_t n, int6
 
 // The g-th largest eigenvalue by one group of BIS_W lanes (lane m of the
 // group, shuffle mask grp); see bisect_kernel.
-__device__ __forceinline__ void bisect_group(int g, int m, unsigned grp, const double* __restrict__ d,
-                                             const double* __restrict__ e2,
-                                             const float* __restrict__ d32,
-                                             const float* __restrict__ e2f, int t, int want,
-                                             const double* __restrict__ bounds,
-                                             double* __restrict__ lam_desc,
-                                             double* __restrict__ lam_asc) {
+// W lanes (2 or 4) cut the interval (W+1)-fold per round: fewer lanes do
+// less FP64 work per eigenvalue, more lanes finish in fewer rounds.
+template <int W>
+__device__ __forceinline__ void bisect_group_w(int g, int m, unsigned grp,
+                                               const double* __restrict__ d,
+                                               const double* __restrict__ e2,
+                                               const float* __restrict__ d32,
+                                               const float* __restrict__ e2f, int t, int want,
+                                               const double* __restrict__ bounds,
+                                               double* __restrict__ lam_desc,
+                                               double* __restrict__ lam_asc) {
     const int idx = t - 1 - g;
     const double eps = 2.220446049250313e-16, pivmin = bounds[2], tn = bounds[3];
     const double abstol = eps * tn;
@@ -115,14 +119,14 @@ __device__ __forceinline__ void bisect_group(int g, int m, unsigned grp, const d
         float lf = __double2float_rd(lo), hf = __double2float_ru(hi);
         const float tolf = 64.f * 1.1920929e-7f * (float)tn;
         for (int it = 0; it < 64 && hf - lf > tolf; ++it) {
-            const float h = (hf - lf) * (1.f / (BIS_W + 1));
+            const float h = (hf - lf) * (1.f / (W + 1));
             const float x = lf + h * (float)(m + 1);
             const int below = sturm_count_f(d32, e2f, t, x, pf) <= idx;  // eigenvalue >= x
             // new interval: between the last point with count <= idx and the next
             float nl = lf, nh = hf;
 #pragma unroll
-            for (int u = 0; u < BIS_W; ++u) {
-                const int bu = __shfl_sync(grp, below, u, BIS_W);
+            for (int u = 0; u < W; ++u) {
+                const int bu = __shfl_sync(grp, below, u, W);
                 const float xu = lf + h * (float)(u + 1);
                 if (bu) nl = xu;
                 else if (nh == hf) nh = xu;
@@ -137,20 +141,20 @@ __device__ __forceinline__ void bisect_group(int g, int m, unsigned grp, const d
         const int ok = m < 2 ? (m == 0 ? sturm_count(d, e2, t, xc, pivmin) <= idx
                                        : sturm_count(d, e2, t, xc, pivmin) > idx)
                              : 1;
-        const int oka = __shfl_sync(grp, ok, 0, BIS_W), okb = __shfl_sync(grp, ok, 1, BIS_W);
+        const int oka = __shfl_sync(grp, ok, 0, W), okb = __shfl_sync(grp, ok, 1, W);
         lo = oka ? a : lo;
         hi = okb ? b : hi;
     }
     for (int it = 0; it < 128; ++it) {
         const double tol = 2.0 * eps * fmax(fabs(lo), fabs(hi)) + abstol + pivmin;
         if (hi - lo <= tol) break;
-        const double h = (hi - lo) * (1.0 / (BIS_W + 1));
+        const double h = (hi - lo) * (1.0 / (W + 1));
         const double x = lo + h * (double)(m + 1);
         const int below = sturm_count(d, e2, t, x, pivmin) <= idx;
         double nl = lo, nh = hi;
 #pragma unroll
-        for (int u = 0; u < BIS_W; ++u) {
-            const int bu = __shfl_sync(grp, below, u, BIS_W);
+        for (int u = 0; u < W; ++u) {
+            const int bu = __shfl_sync(grp, below, u, W);
             const double xu = lo + h * (double)(u + 1);
             if (bu) nl = xu;
             else if (nh == hi) nh = xu;
@@ -165,6 +169,16 @@ __device__ __forceinline__ void bisect_group(int g, int m, unsigned grp, const d
         lam_asc[want - 1 - g] = v;
     }
 
+}
+
+__device__ __forceinline__ void bisect_group(int g, int m, unsigned grp, const double* __restrict__ d,
+                                             const double* __restrict__ e2,
+                                             const float* __restrict__ d32,
+                                             const float* __restrict__ e2f, int t, int want,
+                                             const double* __restrict__ bounds,
+                                             double* __restrict__ lam_desc,
+                                             double* __restrict__ lam_asc) {
+    bisect_group_w<BIS_W>(g, m, grp, d, e2, d32, e2f, t, want, bounds, lam_desc, lam_asc);
 }
 
 // Inverse iteration for vector g; see stein_kernel.
@@ -315,8 +329,8 @@ __device__ __forceinline__ void wy_group(int64_t q, int lane, const cplx* __rest
         for (int c = 0; c < BT_G; ++c)
 #pragma unroll
             for (int r = c + 1; r < BT_G; ++r) {
-                sre[c][r] += v[c].x * v[r].x + v[c].y * v[r].y;
-                sim[c][r] += v[c].x * v[r].y - v[c].y * v[r].x;
+                sre[c][r] = fma(v[c].x, v[r].x, fma(v[c].y, v[r].y, sre[c][r]));
+                sim[c][r] = fma(v[c].x, v[r].y, fma(-v[c].y, v[r].x, sim[c][r]));
             }
     }
 #pragma unroll
@@ -368,9 +382,9 @@ __device__ __forceinline__ void bt_column(int64_t c, int lane, const cplx* __res
 #pragma unroll
             for (int r = 0; r < BT_G; ++r) {
                 if (r < nr) {
-                    const cplx v = refl(A, n, a + r, i);
-                    sr[r] += v.x * xi.x + v.y * xi.y;  // conj(v) x
-                    si[r] += v.x * xi.y - v.y * xi.x;
+                    const cplx v = refl(A, n, a + r, i);  // conj(v) x as two FMA chains
+                    sr[r] = fma(v.x, xi.x, fma(v.y, xi.y, sr[r]));
+                    si[r] = fma(v.x, xi.y, fma(-v.y, xi.x, si[r]));
                 }
             }
         }
@@ -393,7 +407,11 @@ __device__ __forceinline__ void bt_column(int64_t c, int lane, const cplx* __res
             cplx xi = x[i];
 #pragma unroll
             for (int r = 0; r < BT_G; ++r)
-                if (r < nr) xi = csub(xi, cmul(u[r], refl(A, n, a + r, i)));
+                if (r < nr) {  // x -= u v, fused
+                    const cplx v = refl(A, n, a + r, i);
+                    xi.x = fma(-u[r].x, v.x, fma(u[r].y, v.y, xi.x));
+                    xi.y = fma(-u[r].x, v.y, fma(-u[r].y, v.x, xi.y));
+                }
             x[i] = xi;
         }
         __syncwarp();

@@ -140,11 +140,53 @@ struct Sh {
     int flag;  // status of the running trajectory
     int k;     // broadcast of a kept dimension
     double sc[4];
-    double ws[32];
     cplx c[4];
-    double red[8][2 * QJ_DMAX * QJ_DMAX];
-    cplx buf[3 * QJ_GMAX + QT];  // tridiagonal-reduction vectors; bounds and QR scratch
+    double rd[2][QT];  // block reductions: one value per thread, summed by warp 0
+    double res[2];
+    cplx buf[3 * QJ_GMAX + QT];  // tridiagonal-reduction vectors; bounds, QR and BT scratch
 };
+
+// Block sums through shared memory: every thread stores its value, warp 0
+// adds eight per lane and one warp_sum, and the total comes back through
+// shared memory.  Twelve FP64 warp-instructions per sum where a shuffle
+// butterfly in every warp takes eighty, on a pipe that issues two FP64
+// lane-operations per clock per SM.
+__device__ __forceinline__ double bsum(double v, Sh& sh) {
+    sh.rd[0][threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double a = 0.0, b = 0.0;
+#pragma unroll
+        for (int q = 0; q < QT / 32; q += 2) {
+            a += sh.rd[0][threadIdx.x + 32 * q];
+            b += sh.rd[0][threadIdx.x + 32 * (q + 1)];
+        }
+        a = warp_sum(a + b);
+        if (threadIdx.x == 0) sh.res[0] = a;
+    }
+    __syncthreads();
+    return sh.res[0];
+}
+
+__device__ __forceinline__ void bsum2(double u, double v, Sh& sh, double& su, double& sv) {
+    sh.rd[0][threadIdx.x] = u;
+    sh.rd[1][threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        double a = 0.0, b = 0.0;
+#pragma unroll
+        for (int q = 0; q < QT / 32; q += 2) {
+            a += sh.rd[w][l + 32 * q];
+            b += sh.rd[w][l + 32 * (q + 1)];
+        }
+        a = warp_sum(a + b);
+        if (l == 0) sh.res[w] = a;
+    }
+    __syncthreads();
+    su = sh.res[0];
+    sv = sh.res[1];
+}
 
 struct TruncD {
     double cutoff;
@@ -306,9 +348,9 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
     for (int i = tid; i < n; i += QT) {
         const cplx a = A[i];
         vc[i] = a;
-        if (i >= 2) nrm2 += a.x * a.x + a.y * a.y;
+        if (i >= 2) nrm2 = fma(a.x, a.x, fma(a.y, a.y, nrm2));
     }
-    nrm2 = block_sum(nrm2, sh.ws);
+    nrm2 = bsum(nrm2, sh);
     for (int j = 0; j + 1 < n; ++j) {
         if (tid == 0) {
             // reflector with H^H x = beta e_1, beta real (LAPACK zlarfg's convention)
@@ -369,8 +411,7 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
             dre = t.x;
             dim = t.y;
         }
-        dre = block_sum(dre, sh.ws);
-        dim = block_sum(dim, sh.ws);
+        bsum2(dre, dim, sh, dre, dim);
         // w = y - (tau/2) (y^H v) v
         const cplx al2 = cmul(cmk(-0.5 * tv.x, -0.5 * tv.y), cmk(dre, dim));
         if (tid < cr) wp[j + 1 + tid] = cfma(al2, vc[j + 1 + tid], yi);
@@ -390,9 +431,9 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
             a.x -= wi.x + (vi.x * wj1.x + vi.y * wj1.y);
             a.y -= wi.y + (vi.y * wj1.x - vi.x * wj1.y);
             vc[i] = a;
-            if (i >= j + 3) nrm2 += a.x * a.x + a.y * a.y;
+            if (i >= j + 3) nrm2 = fma(a.x, a.x, fma(a.y, a.y, nrm2));
         }
-        nrm2 = block_sum(nrm2, sh.ws);
+        nrm2 = bsum(nrm2, sh);
     }
     if (tid == 0) d[n - 1] = vc[n - 1].x;
     __syncthreads();
@@ -400,19 +441,21 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
 
 // Householder QR of Z (t x k, real, descending eigenvalues) by one block:
 // reflectors in place, scalars qtau, R's diagonal rdiag (qr_kernel's steps).
-__device__ __noinline__ void qr_blk(double* __restrict__ Z, int t, int k, double* __restrict__ qtau,
+// One thread per trailing column: its dot product and update run down the
+// column without shuffles.
+__device__ void qr_blk(double* __restrict__ Z, int t, int k, double* __restrict__ qtau,
                        double* __restrict__ rdiag, Sh& sh) {
     double* sq = reinterpret_cast<double*>(sh.buf);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = QT / 32;
+    const int tid = threadIdx.x;
     for (int j = 0; j < k; ++j) {
         const double* zj = Z + (size_t)j * t;
         double nrm2 = 0.0;
         for (int i = j + tid; i < t; i += QT) {
             const double v = zj[i];
             sq[i] = v;
-            if (i > j) nrm2 += v * v;
+            if (i > j) nrm2 = fma(v, v, nrm2);
         }
-        nrm2 = block_sum(nrm2, sh.ws);
+        nrm2 = bsum(nrm2, sh);
         if (tid == 0) {
             const double al = sq[j];
             double tv = 0.0, beta = al, scale = 0.0;
@@ -433,19 +476,164 @@ __device__ __noinline__ void qr_blk(double* __restrict__ Z, int t, int k, double
         __syncthreads();
         for (int i = j + 1 + tid; i < t; i += QT) Z[i + (size_t)j * t] = sq[i];
         if (tv != 0.0) {
-            for (int c = j + 1 + warp; c < k; c += nw) {
+            for (int c = j + 1 + tid; c < k; c += QT) {
                 double* zc = Z + (size_t)c * t;
                 double s0 = 0.0, s1 = 0.0;
-                int i = j + lane;
-                for (; i + 32 < t; i += 64) {
+                int i = j;
+                for (; i + 1 < t; i += 2) {
                     s0 = fma(sq[i], zc[i], s0);
-                    s1 = fma(sq[i + 32], zc[i + 32], s1);
+                    s1 = fma(sq[i + 1], zc[i + 1], s1);
                 }
                 if (i < t) s0 = fma(sq[i], zc[i], s0);
-                double s = warp_sum(s0 + s1);
-                s = __shfl_sync(0xffffffffu, s, 0) * tv;
-                for (int i2 = j + lane; i2 < t; i2 += 32) zc[i2] -= s * sq[i2];
+                const double f = (s0 + s1) * tv;
+                for (int i2 = j; i2 < t; ++i2) zc[i2] = fma(-f, sq[i2], zc[i2]);
             }
+        }
+        __syncthreads();
+    }
+}
+
+// Column c of the explicit Q (t x k) from qr_blk's reflectors, by one
+// thread: H_0 ... H_c e_c, signed like the input column (qr_form_kernel).
+__device__ __forceinline__ void qr_form_thread(int c, const double* __restrict__ Zr, int t,
+                                               const double* __restrict__ qtau,
+                                               const double* __restrict__ rdiag,
+                                               double* __restrict__ Q) {
+    double* q = Q + (size_t)c * t;
+    for (int i = 0; i < t; ++i) q[i] = (i == c) ? 1.0 : 0.0;
+    for (int j = c; j >= 0; --j) {
+        const double tv = qtau[j];
+        if (tv == 0.0) continue;
+        const double* v = Zr + (size_t)j * t;  // v[j] = 1 implicit
+        double s0 = q[j], s1 = 0.0;
+        int i = j + 1;
+        for (; i + 1 < t; i += 2) {
+            s0 = fma(v[i], q[i], s0);
+            s1 = fma(v[i + 1], q[i + 1], s1);
+        }
+        if (i < t) s0 = fma(v[i], q[i], s0);
+        const double f = (s0 + s1) * tv;
+        q[j] -= f;
+        for (int i2 = j + 1; i2 < t; ++i2) q[i2] = fma(-f, v[i2], q[i2]);
+    }
+    if (rdiag[c] < 0.0)
+        for (int i = 0; i < t; ++i) q[i] = -q[i];
+}
+
+// Compact-WY factor T of reflector group q by one thread (wy_factor_kernel's
+// T[r][r] = tau_r, T[0:r, r] = -tau_r T[0:r, 0:r] V^H v_r).
+__device__ __forceinline__ void wy_thread(int q, const cplx* __restrict__ A, int n,
+                                          const cplx* __restrict__ tau, cplx* __restrict__ Tg) {
+    const int a = q * BT_G;
+    const int nr = min(BT_G, (n - 1) - a);
+    cplx S[BT_G][BT_G];
+#pragma unroll
+    for (int c = 0; c < BT_G; ++c)
+#pragma unroll
+        for (int r = 0; r < BT_G; ++r) S[c][r] = cmk(0, 0);
+    for (int i = a + 1; i < n; ++i) {
+        cplx v[BT_G];
+#pragma unroll
+        for (int r = 0; r < BT_G; ++r) v[r] = r < nr ? refl(A, n, a + r, i) : cmk(0, 0);
+#pragma unroll
+        for (int c = 0; c < BT_G; ++c)
+#pragma unroll
+            for (int r = c + 1; r < BT_G; ++r) {
+                S[c][r].x = fma(v[c].x, v[r].x, fma(v[c].y, v[r].y, S[c][r].x));
+                S[c][r].y = fma(v[c].x, v[r].y, fma(-v[c].y, v[r].x, S[c][r].y));
+            }
+    }
+    cplx T[BT_G][BT_G];
+#pragma unroll
+    for (int c = 0; c < BT_G; ++c)
+#pragma unroll
+        for (int r = 0; r < BT_G; ++r) T[c][r] = cmk(0, 0);
+    for (int r = 0; r < nr; ++r) {
+        const cplx tr = tau[a + r];
+        T[r][r] = tr;
+        cplx z[BT_G];
+        for (int c = 0; c < r; ++c) z[c] = cmul(cmk(-tr.x, -tr.y), S[c][r]);
+        for (int c = 0; c < r; ++c) {
+            cplx acc = cmk(0, 0);
+            for (int u = c; u < r; ++u) acc = cfma(T[c][u], z[u], acc);
+            T[c][r] = acc;
+        }
+    }
+    for (int c = 0; c < BT_G; ++c)
+        for (int r = 0; r < BT_G; ++r) Tg[q * BT_G * BT_G + c + BT_G * r] = T[c][r];
+}
+
+// X = H_0 ... H_{n-2} Q (n x k, Q real) by the whole block, one reflector
+// group at a time from the last: S = V^H X (a thread per (reflector,
+// column) pair, each a dot product down the column), U = T S (a thread per
+// column), X -= V U (a thread per element).  No shuffles.
+__device__ void bt_blk(const cplx* __restrict__ A, int n, const cplx* __restrict__ Tg,
+                       const double* __restrict__ Q, int k, cplx* __restrict__ X, Sh& sh) {
+    cplx* S = sh.buf;  // BT_G x k, k <= QJ_GMAX
+    const int tid = threadIdx.x;
+    for (int e = tid; e < n * k; e += QT) X[e] = cmk(Q[e], 0.0);
+    __syncthreads();
+    const int ngroups = (n - 1 + BT_G - 1) / BT_G;
+    for (int q = ngroups - 1; q >= 0; --q) {
+        const int a = q * BT_G;
+        const int nr = min(BT_G, (n - 1) - a);
+        for (int p = tid; p < nr * k; p += QT) {
+            const int r = p % nr, c = p / nr;
+            const cplx* x = X + (size_t)c * n;
+            double sr0 = 0.0, si0 = 0.0, sr1 = 0.0, si1 = 0.0;
+            int i = a + 1 + r;  // v_r[i] = 0 above a + r + 1
+            {
+                const cplx xi = x[i];  // v_r[a + r + 1] = 1
+                sr0 = xi.x;
+                si0 = xi.y;
+                ++i;
+            }
+            for (; i + 1 < n; i += 2) {
+                const cplx v0 = A[i + (size_t)n * (a + r)], x0 = x[i];
+                const cplx v1 = A[i + 1 + (size_t)n * (a + r)], x1 = x[i + 1];
+                sr0 = fma(v0.x, x0.x, fma(v0.y, x0.y, sr0));
+                si0 = fma(v0.x, x0.y, fma(-v0.y, x0.x, si0));
+                sr1 = fma(v1.x, x1.x, fma(v1.y, x1.y, sr1));
+                si1 = fma(v1.x, x1.y, fma(-v1.y, x1.x, si1));
+            }
+            if (i < n) {
+                const cplx v0 = A[i + (size_t)n * (a + r)], x0 = x[i];
+                sr0 = fma(v0.x, x0.x, fma(v0.y, x0.y, sr0));
+                si0 = fma(v0.x, x0.y, fma(-v0.y, x0.x, si0));
+            }
+            S[r + BT_G * c] = cmk(sr0 + sr1, si0 + si1);
+        }
+        __syncthreads();
+        const cplx* T = Tg + q * BT_G * BT_G;
+        for (int c = tid; c < k; c += QT) {  // U = T S, T upper triangular
+            cplx s[BT_G], u[BT_G];
+#pragma unroll
+            for (int r = 0; r < BT_G; ++r) s[r] = r < nr ? S[r + BT_G * c] : cmk(0, 0);
+#pragma unroll
+            for (int r = 0; r < BT_G; ++r) {
+                cplx acc = cmk(0, 0);
+#pragma unroll
+                for (int v = r; v < BT_G; ++v) acc = cfma(T[r + BT_G * v], s[v], acc);
+                u[r] = acc;
+            }
+#pragma unroll
+            for (int r = 0; r < BT_G; ++r)
+                if (r < nr) S[r + BT_G * c] = u[r];
+        }
+        __syncthreads();
+        const int rows = n - (a + 1);
+        for (int e = tid; e < rows * k; e += QT) {
+            const int i = a + 1 + e % rows, c = e / rows;
+            cplx xi = X[i + (size_t)n * c];
+#pragma unroll
+            for (int r = 0; r < BT_G; ++r) {
+                if (r < nr && i >= a + r + 1) {
+                    const cplx v = refl(A, n, a + r, i), u = S[r + BT_G * c];
+                    xi.x = fma(-u.x, v.x, fma(u.y, v.y, xi.x));
+                    xi.y = fma(-u.x, v.y, fma(-u.y, v.x, xi.y));
+                }
+            }
+            X[i + (size_t)n * c] = xi;
         }
         __syncthreads();
     }
@@ -456,7 +644,7 @@ __device__ __noinline__ void qr_blk(double* __restrict__ Z, int t, int k, double
 __device__ __noinline__ void eig_blk(Traj& T, cplx* G, int n, int want) {
     Scr& s = T.s;
     Sh& sh = *T.sh;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = QT / 32;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (n >= 2) {
         hetrd_blk(G, n, s.d, s.e, s.tau, sh);
     } else {
@@ -468,11 +656,12 @@ __device__ __noinline__ void eig_blk(Traj& T, cplx* G, int n, int want) {
         tri_bounds_block(s.d, s.e, n, s.bounds, s.d32, s.e2f, s.e2, b3, b3 + QT, b3 + 2 * QT);
         __syncthreads();
     }
-    for (int base = 0; base < want * BIS_W; base += QT) {
-        const int gt = base + tid, g = gt / BIS_W, m = gt % BIS_W;
-        const unsigned grp = 0xFu << (lane & ~(BIS_W - 1));
-        if (g < want) bisect_group(g, m, grp, s.d, s.e2, s.d32, s.e2f, n, want, s.bounds, s.lamd,
-                                   s.lama);
+    // two lanes per eigenvalue: 27 % fewer FP64 Sturm counts than four
+    for (int base = 0; base < want * 2; base += QT) {
+        const int gt = base + tid, g = gt / 2, m = gt % 2;
+        const unsigned grp = 0x3u << (lane & ~1);
+        if (g < want)
+            bisect_group_w<2>(g, m, grp, s.d, s.e2, s.d32, s.e2f, n, want, s.bounds, s.lamd, s.lama);
     }
     __syncthreads();
     if (tid == 0) separate_shifts_serial(s.lamd, want, s.bounds, s.shift);
@@ -483,16 +672,14 @@ __device__ __noinline__ void eig_blk(Traj& T, cplx* G, int n, int want) {
     __syncthreads();
     if (want > 1) {
         qr_blk(s.Z, n, want, s.qtau, s.rdiag, sh);
-        for (int w = warp; w < want; w += nw) qr_form_column(w, lane, s.Z, n, want, s.qtau, s.rdiag, s.Q);
+        for (int c = tid; c < want; c += QT) qr_form_thread(c, s.Z, n, s.qtau, s.rdiag, s.Q);
     } else {
         for (int i = tid; i < n; i += QT) s.Q[i] = s.Z[i];
     }
-    __syncthreads();
     const int ngroups = (n - 1 + BT_G - 1) / BT_G;
-    for (int q = warp; q < ngroups; q += nw) wy_group(q, lane, G, n, s.tau, s.wyT);
+    for (int q = tid; q < ngroups; q += QT) wy_thread(q, G, n, s.tau, s.wyT);
     __syncthreads();
-    for (int c = warp; c < want; c += nw) bt_column(c, lane, G, n, s.wyT, ngroups, s.Q, s.V);
-    __syncthreads();
+    bt_blk(G, n, s.wyT, s.Q, want, s.V, sh);
 }
 
 // Keep rule (src/tensors.jl:200-215) on the ascending top eigenvalues lam
@@ -530,7 +717,7 @@ __device__ __noinline__ int split_blk(Traj& T, const cplx* th, int m, int n, boo
     T.fl += 4.0 * g * (g + 1) * (double)(left_iso ? n : m);  // lower triangle
     double trace = 0.0;
     for (int i = threadIdx.x; i < g; i += QT) trace += s.G[i + (size_t)g * i].x;
-    trace = block_sum(trace, sh.ws);
+    trace = bsum(trace, sh);
     const int maxd = (tr.maxdim <= 0 || tr.maxdim > sz) ? sz : tr.maxdim;
     const int want = min(sz, max(maxd, tr.mindim));
     eig_blk(T, s.G, g, want);
@@ -660,8 +847,8 @@ __device__ __noinline__ void normalize(Traj& T) {
     const int c = sh.center, n = T.dl(c) * T.p->d * T.dr(c);
     cplx* A = T.A(c);
     double n2 = 0.0;
-    for (int e = threadIdx.x; e < n; e += QT) n2 += A[e].x * A[e].x + A[e].y * A[e].y;
-    n2 = block_sum(n2, sh.ws);
+    for (int e = threadIdx.x; e < n; e += QT) n2 = fma(A[e].x, A[e].x, fma(A[e].y, A[e].y, n2));
+    n2 = bsum(n2, sh);
     const double inv = 1.0 / sqrt(n2);
     for (int e = threadIdx.x; e < n; e += QT) A[e] = cmk(A[e].x * inv, A[e].y * inv);
     __syncthreads();
@@ -694,19 +881,34 @@ __device__ __noinline__ void rho_contract_t(const cplx* __restrict__ A, const cp
                 acc[2 * q + 1] = fma(x[s].x, y[s2].y, fma(-x[s].y, y[s2].x, acc[2 * q + 1]));
             }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // 8 sums at a time through shared memory: 64 threads add 32 each, 8 add 8
+    double* part = reinterpret_cast<double*>(sh.buf);  // QT x 8 values, then 64 partials
 #pragma unroll
-    for (int q = 0; q < 2 * D * D; ++q) {
-        const double v = warp_sum(acc[q]);
-        if (lane == 0) sh.red[warp][q] = v;
-    }
-    __syncthreads();
-    if ((int)threadIdx.x < 2 * D * D) {
+    for (int q0 = 0; q0 < 2 * D * D; q0 += 8) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q0 + q < 2 * D * D) part[threadIdx.x + QT * q] = acc[q0 + q];
+        __syncthreads();
         double v = 0.0;
-        for (int w = 0; w < QT / 32; ++w) v += sh.red[w][threadIdx.x];
-        reinterpret_cast<double*>(rho)[threadIdx.x] = v;
+        if (threadIdx.x < 64) {
+            const int q = threadIdx.x & 7, h = threadIdx.x >> 3;
+            double a = 0.0, b = 0.0;
+            for (int i = h * 32; i < h * 32 + 32; i += 2) {
+                a += part[i + QT * q];
+                b += part[i + 1 + QT * q];
+            }
+            v = a + b;
+        }
+        __syncthreads();
+        if (threadIdx.x < 64) part[threadIdx.x] = v;
+        __syncthreads();
+        if (threadIdx.x < 8 && q0 + (int)threadIdx.x < 2 * D * D) {
+            double t = 0.0;
+            for (int h = 0; h < 8; ++h) t += part[threadIdx.x + 8 * h];
+            reinterpret_cast<double*>(rho)[q0 + threadIdx.x] = t;
+        }
+        __syncthreads();
     }
-    __syncthreads();
 }
 
 __device__ void rho_contract(const cplx* A, const cplx* Y, int Dl, int d, int Dr, cplx* rho,
