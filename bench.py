@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--qjmc-steps", type=int, default=500, help="qjmc: steps per trajectory")
     p.add_argument("--qjmc-single", type=int, default=2,
                    help="qjmc: trajectories of the one-at-a-time arm")
-    p.add_argument("--blocks-per-sm", type=int, default=2, help="qjmc: engine blocks per SM")
+    p.add_argument("--blocks-per-sm", type=int, default=4, help="qjmc: engine blocks per SM")
     p.add_argument("--qjmc-pre", type=int, default=0,
                    help="qjmc: start every trajectory from one trajectory evolved this many "
                         "steps (untimed) instead of the all-up state")
@@ -74,6 +74,9 @@ def parse():
     p.add_argument("--segments", type=int, default=100, help="tebd-grad: h segments")
     p.add_argument("--fd-coords", type=int, default=2,
                    help="tebd-grad: coordinates checked by central differences")
+    p.add_argument("--fd-k", default="", help="tebd-grad: explicit coordinates (comma list)")
+    p.add_argument("--fd-eps", default="1e-6",
+                   help="tebd-grad: central-difference steps (comma list)")
     return p.parse_args()
 
 
@@ -568,7 +571,8 @@ def tebd_grad_run(args):
     [0, 1], numpy PCG64 seed 5), dt=0.02, real time, 2nd order, maxdim 128,
     cutoff 1e-10, all-up start; objective <Z_16>(T).  Times the forward alone
     and the adjoint gradient (checkpoint every 10 steps); checks `fd_coords`
-    coordinates by central differences (step 1e-6) of the same forward."""
+    coordinates (or --fd-k) by central differences (steps --fd-eps, default
+    1e-6) of the same forward."""
     import tngpu as tn
     N, nsub, dt, chi, site = 32, 5, 0.02, 128, 16
     h = np.random.default_rng(5).uniform(0.0, 1.0, args.segments)
@@ -596,15 +600,19 @@ def tebd_grad_run(args):
     clocks = clk.stop()
     log(f"tebd-grad: forward {t_fwd:.1f} s, gradient {t_grad:.1f} s, f={f:.12f}")
     fd = []
-    eps = 1e-6
-    for k in np.linspace(0, args.segments - 1, args.fd_coords).astype(int) if args.fd_coords else []:
-        hp, hm = h.copy(), h.copy()
-        hp[k] += eps
-        hm[k] -= eps
-        d = (prob.value(psi0, hp) - prob.value(psi0, hm)) / (2 * eps)
-        fd.append({"k": int(k), "adjoint": float(g[k]), "central_difference": d,
-                   "rel_err": abs(g[k] - d) / max(np.max(np.abs(g)), 1e-300)})
-        log(f"tebd-grad fd: {fd[-1]}")
+    if args.fd_k:
+        ks = [int(x) for x in args.fd_k.split(",")]
+    else:
+        ks = np.linspace(0, args.segments - 1, args.fd_coords).astype(int) if args.fd_coords else []
+    for k in ks:
+        for eps in [float(x) for x in args.fd_eps.split(",")]:
+            hp, hm = h.copy(), h.copy()
+            hp[k] += eps
+            hm[k] -= eps
+            d = (prob.value(psi0, hp) - prob.value(psi0, hm)) / (2 * eps)
+            fd.append({"k": int(k), "eps": eps, "adjoint": float(g[k]), "central_difference": d,
+                       "rel_err": abs(g[k] - d) / max(np.max(np.abs(g)), 1e-300)})
+            log(f"tebd-grad fd: {fd[-1]}")
     line = {"metric": "differentiated TEBD gradient wall time", "value": t_grad, "unit": "s",
             "n_gpus": 1, "higher_is_better": False, "dtype": "c128 (f64)", "data": "synthetic",
             "config": {"workload": f"N={N} chain, H = sum ZZ + h_k sum X, {args.segments} segments x "

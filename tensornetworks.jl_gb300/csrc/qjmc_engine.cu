@@ -16,9 +16,10 @@
 //
 // GB300 issues FP64 at two FMAs per clock per SM.  A block's contractions,
 // Gram products, tridiagonal reduction and back-transformation keep that pipe
-// busy from L1/L2-resident operands (a slot's scratch is a few MB), and two or
-// more blocks per SM overlap one block's latency-bound phases (bisection,
-// inverse iteration, keep rule, reductions) with another's FMA phases.
+// busy from L1/L2-resident operands (a slot's scratch is a few MB), and four
+// 128-thread blocks per SM overlap one block's latency-bound phases
+// (bisection, inverse iteration, keep rule, reductions) with the others' FMA
+// phases.
 #include <cmath>
 #include <memory>
 
@@ -35,7 +36,7 @@ namespace {
 
 using namespace eigdev;
 
-constexpr int QT = 256;        // threads per trajectory block
+constexpr int QT = 128;        // threads per trajectory block
 constexpr int QJ_GMAX = 256;   // largest Gram order: d x bond dimension
 constexpr int QJ_NMAX = 1024;  // most sites
 constexpr int QJ_DMAX = 4;     // largest physical dimension
@@ -143,7 +144,7 @@ struct Sh {
     cplx c[4];
     double rd[2][QT];  // block reductions: one value per thread, summed by warp 0
     double res[2];
-    cplx buf[3 * QJ_GMAX + QT];  // tridiagonal-reduction vectors; bounds, QR and BT scratch
+    cplx buf[4 * QJ_GMAX + QT];  // tridiagonal-reduction vectors; bounds, QR and BT scratch
 };
 
 // Block sums through shared memory: every thread stores its value, warp 0
@@ -342,6 +343,7 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
     cplx* wp = sh.buf + QJ_GMAX;
     cplx* vc = sh.buf + 2 * QJ_GMAX;
     cplx* red = sh.buf + 3 * QJ_GMAX;
+    cplx* ys = sh.buf + 3 * QJ_GMAX + QT;
     const int tid = threadIdx.x;
     bool pend = false;
     double nrm2 = 0.0;
@@ -375,46 +377,50 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
         for (int i = j + 2 + tid; i < n; i += QT) vc[i] = cmul(vc[i], scale);
         if (tid == 0) vc[j + 1] = cmk(1, 0);
         __syncthreads();
-        // rows and columns j+1..n-1: pending update, then y = tau A v
-        const int m = n - j - 1;  // m < QJ_GMAX <= QT: one pass covers every row
-        const int cr = m, cs = QT / cr;
-        double ar = 0.0, ai = 0.0;
-        if (tid < cs * cr) {
-            const int i = j + 1 + tid % cr;
-            const cplx vpi = pend ? vp[i] : cmk(0, 0), wpi = pend ? wp[i] : cmk(0, 0);
-            for (int l = j + 1 + tid / cr; l < n; l += cs) {
-                cplx a = A[i + (size_t)n * l];
-                if (pend) {
-                    const cplx vl = vp[l], wl = wp[l];
-                    a.x = fma(-wpi.x, vl.x, fma(-wpi.y, vl.y, fma(-vpi.x, wl.x, fma(-vpi.y, wl.y, a.x))));
-                    a.y = fma(-wpi.y, vl.x, fma(wpi.x, vl.y, fma(-vpi.y, wl.x, fma(vpi.x, wl.y, a.y))));
-                    A[i + (size_t)n * l] = a;
-                }
-                const cplx x = vc[l];
-                ar = fma(a.x, x.x, fma(-a.y, x.y, ar));
-                ai = fma(a.x, x.y, fma(a.y, x.x, ai));
-            }
-        }
-        red[tid] = cmk(ar, ai);
-        __syncthreads();
-        int span = 1;
-        while (span < cs) span <<= 1;
-        for (int h = span >> 1; h > 0; h >>= 1) {
-            if (tid < h * cr && tid + h * cr < cs * cr) red[tid] = cadd(red[tid], red[tid + h * cr]);
-            __syncthreads();
-        }
-        cplx yi = cmk(0, 0);
+        // rows and columns j+1..n-1, up to QT rows per pass: pending update,
+        // then y = tau A v
+        const int m = n - j - 1;
         double dre = 0.0, dim = 0.0;
-        if (tid < cr) {
-            yi = cmul(tv, red[tid]);
-            const cplx t = cmul(cconj(yi), vc[j + 1 + tid]);  // y^H v
-            dre = t.x;
-            dim = t.y;
+        for (int rb = 0; rb < m; rb += QT) {
+            const int cr = min(m - rb, QT), cs = QT / cr;
+            double ar = 0.0, ai = 0.0;
+            if (tid < cs * cr) {
+                const int i = j + 1 + rb + tid % cr;
+                const cplx vpi = pend ? vp[i] : cmk(0, 0), wpi = pend ? wp[i] : cmk(0, 0);
+                for (int l = j + 1 + tid / cr; l < n; l += cs) {
+                    cplx a = A[i + (size_t)n * l];
+                    if (pend) {
+                        const cplx vl = vp[l], wl = wp[l];
+                        a.x = fma(-wpi.x, vl.x, fma(-wpi.y, vl.y, fma(-vpi.x, wl.x, fma(-vpi.y, wl.y, a.x))));
+                        a.y = fma(-wpi.y, vl.x, fma(wpi.x, vl.y, fma(-vpi.y, wl.x, fma(vpi.x, wl.y, a.y))));
+                        A[i + (size_t)n * l] = a;
+                    }
+                    const cplx x = vc[l];
+                    ar = fma(a.x, x.x, fma(-a.y, x.y, ar));
+                    ai = fma(a.x, x.y, fma(a.y, x.x, ai));
+                }
+            }
+            red[tid] = cmk(ar, ai);
+            __syncthreads();
+            int span = 1;
+            while (span < cs) span <<= 1;
+            for (int h = span >> 1; h > 0; h >>= 1) {
+                if (tid < h * cr && tid + h * cr < cs * cr) red[tid] = cadd(red[tid], red[tid + h * cr]);
+                __syncthreads();
+            }
+            if (tid < cr) {
+                const cplx yi = cmul(tv, red[tid]);
+                ys[rb + tid] = yi;
+                const cplx t = cmul(cconj(yi), vc[j + 1 + rb + tid]);  // y^H v
+                dre += t.x;
+                dim += t.y;
+            }
+            __syncthreads();
         }
         bsum2(dre, dim, sh, dre, dim);
         // w = y - (tau/2) (y^H v) v
         const cplx al2 = cmul(cmk(-0.5 * tv.x, -0.5 * tv.y), cmk(dre, dim));
-        if (tid < cr) wp[j + 1 + tid] = cfma(al2, vc[j + 1 + tid], yi);
+        for (int r = tid; r < m; r += QT) wp[j + 1 + r] = cfma(al2, vc[j + 1 + r], ys[r]);
         for (int i = j + 2 + tid; i < n; i += QT) A[i + (size_t)n * j] = vc[i];
         cplx* t = vp;  // v_j becomes the pending vector
         vp = vc;
@@ -424,8 +430,8 @@ __device__ __noinline__ void hetrd_blk(cplx* __restrict__ A, int n, double* __re
         // column j+1 with this step's update (v_{j+1} = 1)
         const cplx wj1 = wp[j + 1];
         nrm2 = 0.0;
-        if (tid < cr) {
-            const int i = j + 1 + tid;
+        for (int r = tid; r < m; r += QT) {
+            const int i = j + 1 + r;
             const cplx vi = vp[i], wi = wp[i];
             cplx a = A[i + (size_t)n * (j + 1)];
             a.x -= wi.x + (vi.x * wj1.x + vi.y * wj1.y);
@@ -881,7 +887,7 @@ __device__ __noinline__ void rho_contract_t(const cplx* __restrict__ A, const cp
                 acc[2 * q + 1] = fma(x[s].x, y[s2].y, fma(-x[s].y, y[s2].x, acc[2 * q + 1]));
             }
     }
-    // 8 sums at a time through shared memory: 64 threads add 32 each, 8 add 8
+    // 8 sums at a time through shared memory: 64 threads add QT/8 each, 8 add 8
     double* part = reinterpret_cast<double*>(sh.buf);  // QT x 8 values, then 64 partials
 #pragma unroll
     for (int q0 = 0; q0 < 2 * D * D; q0 += 8) {
@@ -891,9 +897,9 @@ __device__ __noinline__ void rho_contract_t(const cplx* __restrict__ A, const cp
         __syncthreads();
         double v = 0.0;
         if (threadIdx.x < 64) {
-            const int q = threadIdx.x & 7, h = threadIdx.x >> 3;
+            const int q = threadIdx.x & 7, h = threadIdx.x >> 3, per = QT / 8;
             double a = 0.0, b = 0.0;
-            for (int i = h * 32; i < h * 32 + 32; i += 2) {
+            for (int i = h * per; i < h * per + per; i += 2) {
                 a += part[i + QT * q];
                 b += part[i + 1 + QT * q];
             }
@@ -1103,7 +1109,7 @@ __device__ void run_traj(const QjParams& p, Sh& sh, int t, int slot) {
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(QT, 2) qjmc_engine_kernel(QjParams p) {
+__global__ void __launch_bounds__(QT, 4) qjmc_engine_kernel(QjParams p) {
     __shared__ Sh sh;
     for (int t = blockIdx.x; t < p.ntraj; t += gridDim.x) run_traj(p, sh, t, blockIdx.x);
 }

@@ -400,7 +400,7 @@ end
 function qjmc_ensemble(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, tmax::Real, dt::Real,
                        obs::OpList, ntraj::Integer; seed::Integer=0, first_traj::Integer=0,
                        save::Real=0, cutoff::Real=1e-12, mindim::Int=1, maxdim::Int=64,
-                       blocks_per_sm::Integer=2)
+                       blocks_per_sm::Integer=4)
     save = save == 0 ? dt : save
     steps = Int(ceil(round(tmax / dt, digits=5)))
     savesteps = Int(ceil(round(save / dt)))

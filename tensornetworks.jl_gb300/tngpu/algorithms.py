@@ -374,7 +374,7 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
                   draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
-                  seed=None, first_traj=0, engine="auto", blocks_per_sm=2, records=False,
+                  seed=None, first_traj=0, engine="auto", blocks_per_sm=4, records=False,
                   stats=None):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,

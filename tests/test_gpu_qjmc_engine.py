@@ -9,7 +9,9 @@ launch runs whole quantum-jump trajectories (qjmc.jl:28-220) on the device.
   * Against the host-worker engine (tn_qjmc_batch) on the same seeded
     streams: identical jump counts, averaged <Z_i>(t) to 1e-9.
   * The launch width (blocks per SM) does not change any trajectory.
-  * A draw stream that runs out is reported as an error status."""
+  * A draw stream that runs out is reported as an error status.
+  * Bonds wider than the block's thread count (Gram order 160) still match
+    the oracle."""
 
 import numpy as np
 import pytest
@@ -104,3 +106,32 @@ def test_engine_reports_an_exhausted_stream(tn):
     with pytest.raises(ValueError, match="maxdim"):
         tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, 2, draws=draws, cutoff=1e-10,
                          maxdim=0, engine="device")
+
+
+def test_engine_wide_bonds_match_oracle(tn):
+    """Gram orders above the block's thread count (bond dimension 80: n = 160
+    rows of the tridiagonal reduction, several row passes per step) from a
+    random N=14 MPS: jump records and <Z_i> against the oracle."""
+    N, dt, steps, ntraj, D = 14, 0.05, 3, 3, 80
+    draws = np.random.default_rng(90).random((ntraj, 3 * steps + 3))
+    Ho, Lo, Zo = _model(O, N, g=2.0)
+    po0 = O.random_mps(2, N, D, np.random.default_rng(91))
+    avg, jumps = 0.0, []
+    for t in range(ntraj):
+        po = po0.copy()
+        rec = {}
+        j, _ = O.qjmc_simulation(O.spinhalf(), po, Ho, Lo, steps * dt, dt,
+                                 O.algorithms.UniformStream(draws[t]), [Zo], save=dt,
+                                 cutoff=1e-12, maxdim=D, record=rec)
+        avg = avg + np.real(np.array([r[0] for r in rec["ops"]]))
+        jumps.append(list(j))
+    avg /= ntraj
+    Hg, Lg, Zg = _model(tn, N, g=2.0)
+    st = tn.spinhalf()
+    pg = tn.GMPS.from_tensors(po0.tensors, po0.center)
+    assert max(pg.bonddims()) > 64
+    _, out, nj, jg, _ = tn.qjmc_ensemble(st, pg, Hg, Lg, steps * dt, dt, Zg, ntraj, draws=draws,
+                                         save=dt, cutoff=1e-12, maxdim=D, engine="device",
+                                         records=True)
+    assert [list(map(int, j)) for j in jg] == jumps
+    assert np.allclose(np.real(out), avg, atol=1e-9)
