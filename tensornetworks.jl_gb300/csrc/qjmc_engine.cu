@@ -484,14 +484,16 @@ __device__ void qr_blk(double* __restrict__ Z, int t, int k, double* __restrict_
         if (tv != 0.0) {
             for (int c = j + 1 + tid; c < k; c += QT) {
                 double* zc = Z + (size_t)c * t;
-                double s0 = 0.0, s1 = 0.0;
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // four FMA chains
                 int i = j;
-                for (; i + 1 < t; i += 2) {
+                for (; i + 3 < t; i += 4) {
                     s0 = fma(sq[i], zc[i], s0);
                     s1 = fma(sq[i + 1], zc[i + 1], s1);
+                    s2 = fma(sq[i + 2], zc[i + 2], s2);
+                    s3 = fma(sq[i + 3], zc[i + 3], s3);
                 }
-                if (i < t) s0 = fma(sq[i], zc[i], s0);
-                const double f = (s0 + s1) * tv;
+                for (; i < t; ++i) s0 = fma(sq[i], zc[i], s0);
+                const double f = ((s0 + s1) + (s2 + s3)) * tv;
                 for (int i2 = j; i2 < t; ++i2) zc[i2] = fma(-f, sq[i2], zc[i2]);
             }
         }
@@ -511,14 +513,16 @@ __device__ __forceinline__ void qr_form_thread(int c, const double* __restrict__
         const double tv = qtau[j];
         if (tv == 0.0) continue;
         const double* v = Zr + (size_t)j * t;  // v[j] = 1 implicit
-        double s0 = q[j], s1 = 0.0;
+        double s0 = q[j], s1 = 0.0, s2 = 0.0, s3 = 0.0;
         int i = j + 1;
-        for (; i + 1 < t; i += 2) {
+        for (; i + 3 < t; i += 4) {
             s0 = fma(v[i], q[i], s0);
             s1 = fma(v[i + 1], q[i + 1], s1);
+            s2 = fma(v[i + 2], q[i + 2], s2);
+            s3 = fma(v[i + 3], q[i + 3], s3);
         }
-        if (i < t) s0 = fma(v[i], q[i], s0);
-        const double f = (s0 + s1) * tv;
+        for (; i < t; ++i) s0 = fma(v[i], q[i], s0);
+        const double f = ((s0 + s1) + (s2 + s3)) * tv;
         q[j] -= f;
         for (int i2 = j + 1; i2 < t; ++i2) q[i2] = fma(-f, v[i2], q[i2]);
     }
