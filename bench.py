@@ -158,7 +158,9 @@ def peaks():
 def cpu_bond_sample(chi, w=5, d=2, seed=0):
     """One two-site bond update of the FP64 CPU restatement at chi: Lanczos
     (krylovdim 3, 2 cycles: 5 matvecs), truncated SVD to chi, one environment
-    update.  Environment blocks are Hermitian per channel, synthetic."""
+    update.  The matvecs use the reference's contraction order (left block
+    and MPO tensors first, projmps.jl:103-145), as its CPU path runs them.
+    Environment blocks are Hermitian per channel, synthetic."""
     import oracle as O
     rng = np.random.default_rng(seed)
 
@@ -171,12 +173,21 @@ def cpu_bond_sample(chi, w=5, d=2, seed=0):
     W = O.mpo_from_oplist(st, xxz(O, 8))[4]  # a bulk tensor, w = 5 on both sides
     theta = rng.standard_normal((chi, d, d, chi)) + 1j * rng.standard_normal((chi, d, d, chi))
     t0 = time.perf_counter()
-    _, vec = O.lanczos_lowest(lambda x: O.core.heff2(L, W, W, R, x), theta, 3, 2)
+    _, vec = O.lanczos_lowest(lambda x: O.core.heff2_reference_order(L, W, W, R, x), theta, 3, 2)
     M = O.fr(vec, (chi * d, d * chi))
     U, S, Vt = O.trunc_svd(M, 1e-12, chi, 1)
     A = O.fr(U, (chi, d, U.shape[1]))
     O.core.env_left(L, A, W, A)
     return time.perf_counter() - t0
+
+
+def blas_threads():
+    """The BLAS thread setting of the CPU restatement: the environment's
+    OPENBLAS/OMP variables, else OpenBLAS's default of one thread per core."""
+    for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS"):
+        if os.environ.get(k):
+            return f"{k}={os.environ[k]}"
+    return f"OpenBLAS default ({os.cpu_count()} threads, one per core)"
 
 
 def reference_arm(args):
@@ -197,9 +208,11 @@ def reference_arm(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config(args),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "blas_threads": blas_threads(),
                              "sample": f"one bond update at chi={args.chi} per step (5 Lanczos "
-                                       f"matvecs, SVD, env update), extrapolated x{args.n - 1} "
-                                       "bonds; Julia absent, numpy FP64 restatement"},
+                                       f"matvecs in the reference's contraction order, SVD, env "
+                                       f"update), extrapolated x{args.n - 1} bonds; Julia absent, "
+                                       "numpy FP64 restatement"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -360,10 +373,11 @@ def ours(args):
         t = cpu_bond_sample(args.chi)
         line["cpu_baseline"] = {"value": 1.0 / (t * (args.n - 1)), "unit": UNIT,
                                 "cores": os.cpu_count(), "kind": "port",
-                                "blas_threads": os.environ.get("OPENBLAS_NUM_THREADS", "default"),
+                                "blas_threads": blas_threads(),
                                 "sample": f"one bond update at chi={args.chi} ({t:.1f} s: 5 Lanczos "
-                                          f"matvecs, SVD, env update), x{args.n - 1} bonds; numpy "
-                                          "FP64 restatement (Julia absent)"}
+                                          f"matvecs in the reference's contraction order, SVD, "
+                                          f"env update), x{args.n - 1} bonds; numpy FP64 "
+                                          "restatement (Julia absent)"}
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -544,6 +544,21 @@ def heff2(L, W1, W2, R, theta):
     return np.tensordot(t, R, axes=([3, 4], [1, 2]))          # a p q c'
 
 
+def heff2_reference_order(L, W1, W2, R, theta):
+    """The same product in the reference's contraction order
+    (projmps.jl:103-145, rank-2 branch): the left block is contracted with
+    the MPO tensors first (prod[a, b, s1', s1, s2', s2, w''], chi^2 d^4 w
+    entries; projmps.jl:116-130), then with the two-site tensor over (b, s1,
+    s2) (projmps.jl:133) and with the right block over (w'', c)
+    (projmps.jl:134-135): about 2.5x the flops of heff2's order at chi=1024,
+    w=5.  The CPU baseline times this order."""
+    prod = np.transpose(L, (0, 2, 1))                                   # a b w
+    prod = np.tensordot(prod, W1, axes=([2], [0]))                      # a b s1' s1 w'
+    prod = np.tensordot(prod, W2, axes=([4], [0]))                      # a b s1' s1 s2' s2 w''
+    prod = np.tensordot(prod, theta, axes=([1, 3, 5], [0, 1, 2]))       # a s1' s2' w'' c
+    return np.tensordot(prod, R, axes=([3, 4], [1, 2]))                 # a s1' s2' c'
+
+
 class ProjMPS:
     """Environment blocks of <bra|[MPO]|ket> with a movable centre
     (projmps.jl:16-42, abstractprojmps.jl:33-81).  ``blocks[i]`` (1-based) is

@@ -386,3 +386,17 @@ def test_tebd_with_projector_finds_excited_state():
     v /= np.linalg.norm(v)
     assert abs(X.dense_expect(v, X.oplist_to_dense(st, H)) - ev[1]) < 2e-5
     assert abs(np.vdot(X.mps_to_dense(g), v)) < 1e-6
+
+
+def test_heff2_reference_order_matches_optimal_order():
+    """The reference's contraction order (the CPU baseline's) and the
+    oracle's optimal order give the same two-site product."""
+    rng = np.random.default_rng(12)
+
+    def c(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    L, W1, W2, R, th = c(6, 3, 6), c(3, 2, 2, 4), c(4, 2, 2, 5), c(7, 5, 7), c(6, 2, 2, 7)
+    a = O.core.heff2(L, W1, W2, R, th)
+    b = O.core.heff2_reference_order(L, W1, W2, R, th)
+    assert np.allclose(a, b, rtol=1e-13, atol=1e-12)
