@@ -200,6 +200,14 @@ int32_t tn_vmps(tn_ctx* ctx, int32_t nterms, const tn_mps* const* terms, const d
  * site 1 with the truncation trunc (NULL: none). */
 int32_t tn_mpo_apply(tn_ctx* ctx, const tn_mpo* O, const tn_mps* psi, const tn_trunc_opts* trunc,
                      tn_mps** out);
+/* applyMPO(O1, O2; kwargs) = MPOMPOProduct (mpo.jl:147-167) on MPOs held as
+ * fused MPS handles: physical dimension d^2 with index o + d*i (the
+ * column-major grouping of a rank-2 site [Dl, o, i, Dr], the grouping the
+ * reference's rank-2 SVDs use).  The product O1 O2 (O1's input index summed
+ * with O2's output index) is left-canonicalised, then its centre moved to
+ * site 1 with the truncation trunc (NULL: none). */
+int32_t tn_mpo_mpo_apply(tn_ctx* ctx, const tn_mps* O1, const tn_mps* O2, int32_t d,
+                         const tn_trunc_opts* trunc, tn_mps** out);
 /* psi <- a psi, a complex (re, im): the centre tensor is scaled (site 1
  * without a centre), as *(psi, a) does (abstractmps.jl:100-107). */
 int32_t tn_mps_scale(tn_ctx* ctx, tn_mps* psi, const double* a);

@@ -230,7 +230,17 @@ def trotterize(st, ops, dt, order=2, evol="imag"):
 
 
 def applygate(psi, site, gate, direction=False, cutoff=0.0, maxdim=0, mindim=1):
-    """gatelist.jl:137-171 without the optional fidelity (off in applygates!)."""
+    """gatelist.jl:137-171 without the optional fidelity (off in applygates!).
+    On an MPO (rank 2) the gate acts on each site's output index."""
+    if psi.rank == 2:
+        if gate.ndim == 2:
+            theta = np.einsum("po,aoib->apib", gate, psi[site])
+        else:
+            prod = np.tensordot(psi[site], psi[site + 1], axes=([3], [0]))  # a o1 i1 o2 i2 b
+            theta = np.einsum("pkql,akilmb->apiqmb", gate, prod, optimize=True)
+        psi.replacesites(theta, site, direction, False, cutoff=cutoff, maxdim=maxdim,
+                         mindim=mindim)
+        return
     if gate.ndim == 2:
         theta = np.einsum("ts,asb->atb", gate, psi[site])
     else:

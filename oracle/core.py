@@ -14,7 +14,7 @@ __all__ = [
     "Sitetypes", "spinhalf", "OpList", "svd_keep", "trunc_svd", "GMPS",
     "random_mps", "product_mps", "mpo_from_oplist", "ProjMPS", "inner",
     "applyop", "totensor", "sitetensor", "siterange", "siteindexs", "fr",
-    "ProjMPSSum", "overlap", "scaled", "mpo_mps_product", "MPSProjector",
+    "ProjMPSSum", "overlap", "scaled", "mpo_mps_product", "product_mpo", "adjoint_mpo", "mpo_mpo_product", "trace_mpos", "MPSProjector",
 ]
 
 
@@ -356,7 +356,21 @@ class GMPS:
         site+1.  direction True: SVD of M[(Dl,s1),(s2,Dr)]; left gets U*S,
         right gets Vt; centre = site.  One-site tensors take the nsites == 1
         branch (gmps.jl:204-213)."""
-        if theta.ndim == 3:
+        if self.rank == 2 and theta.ndim == 6:
+            # rank-2 two-site tensor [Dl, o1, i1, o2, i2, Dr]: the SVD groups
+            # (Dl, o1, i1) against (o2, i2, Dr), the fused physical index
+            # o + d i of each site (gmps.jl:199-267 with rank 2)
+            Dl, d, _, _, _, Dr = theta.shape
+            fused = GMPS(1, d * d, [fr(t, (t.shape[0], d * d, t.shape[-1])) for t in self.tensors],
+                         self.center)
+            fused.replacesites(fr(theta, (Dl, d * d, d * d, Dr)), site, direction, False,
+                               cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+            self.tensors = [fr(t, (t.shape[0], d, d, t.shape[-1])) for t in fused.tensors]
+            self.center = fused.center
+            if normalize:
+                self.normalize()
+            return
+        if theta.ndim == 3 or (self.rank == 2 and theta.ndim == 4):
             self[site] = theta
             nxt = site + 1 - 2 * int(direction)
             if 0 < nxt <= len(self):
@@ -557,6 +571,54 @@ def heff2_reference_order(L, W1, W2, R, theta):
     prod = np.tensordot(prod, W2, axes=([4], [0]))                      # a b s1' s1 s2' s2 w''
     prod = np.tensordot(prod, theta, axes=([1, 3, 5], [0, 1, 2]))       # a s1' s2' w'' c
     return np.tensordot(prod, R, axes=([3, 4], [1, 2]))                 # a s1' s2' c'
+
+
+def product_mpo(st, names):
+    """productMPO(st, names) (mpo.jl:85-93): sites [1, d, d, 1] of the named
+    operators, centre unset."""
+    return GMPS(2, st.dim, [fr(st.op(n), (1, st.dim, st.dim, 1)) for n in names], 0)
+
+
+def adjoint_mpo(O):
+    """adjoint(O) (mpo.jl:32-39): every site conjugated with its two physical
+    indices swapped."""
+    out = O.copy()
+    out.tensors = [np.conj(np.transpose(t, (0, 2, 1, 3))) for t in O.tensors]
+    return out
+
+
+def mpo_mpo_product(O1, O2, cutoff=0.0, maxdim=0, mindim=1):
+    """MPOMPOProduct(O1, O2; kwargs) (mpo.jl:147-167): sites
+    M[(a, b), o, i, (a', b')] = sum_k O1[a, o, k, a'] O2[b, k, i, b'] (a
+    fastest in each pair), left-canonicalised while they are built, then the
+    centre moved to site 1 with the truncation."""
+    N = len(O1)
+    ts = []
+    for i in range(1, N + 1):
+        M = np.einsum("aokx,bkiy->aboixy", O1[i], O2[i])
+        da, db, d, _, dx, dy = M.shape
+        ts.append(fr(M, (da * db, d, d, dx * dy)))
+    O = GMPS(2, O1.dim, ts, 0)
+    for i in range(1, N):
+        O.moveright(i)
+    O.center = 0
+    O.movecenter(1, cutoff=cutoff, maxdim=maxdim, mindim=mindim)
+    return O
+
+
+def trace_mpos(*ops):
+    """trace(O1, ..., Ok) = Tr(O1 O2 ... Ok) (mpo.jl:229-252) by a transfer
+    tensor over the k bond indices, site by site."""
+    k = len(ops)
+    letters = "abcdefghij"
+    bonds, nbonds, phys = letters[:k], letters[k:2 * k], "pqrstuvwxy"[:k]
+    E = np.ones((1,) * k, dtype=np.complex128)
+    for site in range(1, len(ops[0]) + 1):
+        # operator j maps physical index phys[j+1] (its input) from phys[j]
+        terms = [f"{bonds[j]}{phys[j]}{phys[(j + 1) % k]}{nbonds[j]}" for j in range(k)]
+        E = np.einsum(f"{bonds}," + ",".join(terms) + f"->{nbonds}", E,
+                      *[op[site] for op in ops])
+    return complex(E.reshape(-1)[0])
 
 
 class ProjMPS:

@@ -49,6 +49,7 @@ struct VmpsResult {
 VmpsResult vmps_run(tn_mps* fit, const std::vector<const tn_mps*>& terms,
                     const std::vector<cplx>& coeffs, const tn_vmps_opts& o);
 void mpo_apply(const tn_mpo* O, const tn_mps* psi, const Trunc& t, tn_mps* out);
+void mpo_mpo_apply(const tn_mps* A, const tn_mps* B, int d, const Trunc& t, tn_mps* out);
 void mps_scale(tn_mps* psi, cplx a);
 cplx mps_overlap(const tn_mps* bra, tn_mps* ket);
 }  // namespace tn
@@ -486,6 +487,22 @@ int32_t tn_mpo_apply(tn_ctx* h, const tn_mpo* O, const tn_mps* psi, const tn_tru
     tn_mps* r = new tn_mps();
     try {
         mpo_apply(O, psi, t ? to_trunc(t) : no_trunc(), r);
+        r->ctx->sync();
+    } catch (...) {
+        delete r;
+        throw;
+    }
+    *out = r;
+    TN_API_END
+}
+
+int32_t tn_mpo_mpo_apply(tn_ctx* h, const tn_mps* A, const tn_mps* B, int32_t d,
+                         const tn_trunc_opts* t, tn_mps** out) {
+    TN_API_BEGIN(h ? &h->c : nullptr)
+    TN_REQUIRE(A && B && out, "null argument");
+    tn_mps* r = new tn_mps();
+    try {
+        mpo_mpo_apply(A, B, d, t ? to_trunc(t) : no_trunc(), r);
         r->ctx->sync();
     } catch (...) {
         delete r;

@@ -36,7 +36,57 @@ __global__ void mpo_mps_site_kernel(const cplx* __restrict__ M, const cplx* __re
     }
 }
 
+// Fused MPO sites (physical index p = o + d i, the column-major grouping of
+// [Dl, o, i, Dr]): out[(a + Da b), (o + d i), (a2 + Da2 b2)] =
+// sum_k A[a, (o + d k), a2] B[b, (k + d i), b2] (MPOMPOProduct, mpo.jl:151-158)
+__global__ void mpo_mpo_site_kernel(const cplx* __restrict__ A, const cplx* __restrict__ B,
+                                    int64_t da, int64_t da2, int64_t db, int64_t db2, int d,
+                                    cplx* __restrict__ out) {
+    const int64_t d2 = (int64_t)d * d, L = da * db, R = da2 * db2, total = L * d2 * R;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t l = e % L, p = (e / L) % d2, r = e / (L * d2);
+        const int64_t a = l % da, b = l / da, a2 = r % da2, b2 = r / da2;
+        const int64_t o = p % d, i = p / d;
+        cplx acc = cmk(0, 0);
+        for (int k = 0; k < d; ++k)
+            acc = cfma(A[a + da * ((o + d * k) + d2 * a2)], B[b + db * ((k + d * i) + d2 * b2)], acc);
+        out[e] = acc;
+    }
+}
+
 }  // namespace
+
+// MPOMPOProduct(O1, O2; trunc) (mpo.jl:147-167) on fused MPOs: MPSs of
+// physical dimension d^2 whose index is (o + d i).  The product's sites are
+// built, left-canonicalised without truncation, then the centre moves to
+// site 1 with the caller's truncation, as for the MPO-MPS product.
+void mpo_mpo_apply(const tn_mps* A, const tn_mps* B, int d, const Trunc& t, tn_mps* out) {
+    TN_REQUIRE(A->N == B->N && A->d == B->d, "GMPS must share the same physical dims.");
+    TN_REQUIRE(d >= 1 && (int64_t)d * d == A->d, "fused MPOs have physical dimension d^2");
+    Ctx* ctx = A->ctx;
+    const int N = A->N, d2 = d * d;
+    out->ctx = ctx;
+    out->N = N;
+    out->d = d2;
+    out->dims.assign(N + 1, 1);
+    out->A.clear();
+    out->A.resize(N);
+    for (int i = 0; i <= N; ++i) out->dims[i] = A->dims[i] * B->dims[i];
+    for (int i = 1; i <= N; ++i) {
+        const int64_t da = A->dl(i), da2 = A->dr(i), db = B->dl(i), db2 = B->dr(i);
+        const int64_t total = da * db * d2 * da2 * db2;
+        out->A[i - 1] = DBuf(ctx, sizeof(cplx) * total);
+        const int64_t g = std::min<int64_t>((total + 255) / 256, (int64_t)ctx->sm_count * 8);
+        mpo_mpo_site_kernel<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, ctx->stream>>>(
+            A->site(i), B->site(i), da, da2, db, db2, d, out->A[i - 1].c());
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+    }
+    out->center = 0;
+    movecenter(out, N, no_trunc());
+    movecenter(out, 1, t);
+}
 
 // psi <- a psi: the centre tensor (site 1 without a centre) is scaled
 // (*(psi, a), abstractmps.jl:100-107).

@@ -3,9 +3,11 @@
 The names mirror the reference's exports (src/exports.jl): ``spinhalf``,
 ``OpList``, ``MPO``, ``randomMPS``, ``productMPS``, ``dmrg``,
 ``trotterize``, ``applygates``, ``tebd``, ``qjmc_simulation``, ``inner``,
-observers.  Every contraction, truncation and eigensolve runs in
+observers, and the MPO algebra (``productMPO``, ``applyMPO``, ``adjoint``,
+``trace``).  Every contraction, truncation and eigensolve runs in
 ``libtngpu.so`` on the GPU; nothing here computes on the CPU beyond building
-model inputs (operator tables, MPO tensors, 4x4 gate exponentials).
+model inputs (operator tables, MPO tensors, 4x4 gate exponentials and their
+output-index lifts) and re-laying out MPO sites for ``adjoint``.
 """
 
 from ._lib import Context, TNError, context, load  # noqa: F401
@@ -15,6 +17,7 @@ from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEB
                          shard_range, tebd,
                          tebd_grad, trotterize, vmps)
 from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
-from .mps import (GMPS, MPO, MPOHandle, MPSProjector, applyMPO, entropy, inner,  # noqa: F401
+from .mps import (GMPO, GMPS, MPO, MPOHandle, MPSProjector, adjoint, applyMPO, as_gmpo,  # noqa: F401
+                  entropy, inner, mpo_product, productMPO, trace,
                   mps_from_record, mps_record, overlap, productMPS, randomMPS, read_mps,
                   write_mps)

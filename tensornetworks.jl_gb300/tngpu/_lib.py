@@ -65,6 +65,7 @@ _SIGS = {
     "tn_vmps": (i32, [P, i32, C.POINTER(P), dp, C.POINTER(VmpsOpts), C.POINTER(P), dp,
                       C.POINTER(i32)]),
     "tn_mpo_apply": (i32, [P, P, P, C.POINTER(TruncOpts), C.POINTER(P)]),
+    "tn_mpo_mpo_apply": (i32, [P, P, P, i32, C.POINTER(TruncOpts), C.POINTER(P)]),
     "tn_mps_scale": (i32, [P, P, dp]),
     "tn_mps_overlap": (i32, [P, P, P, dp]),
     "tn_mpo_upload": (i32, [P, i32, i32, i64p, dpp, C.POINTER(P)]),

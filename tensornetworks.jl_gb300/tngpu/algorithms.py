@@ -146,9 +146,32 @@ def trotterize(st, ops: OpList, dt, order=2, evol="imag", ctx=None):
     return GateList(ops.length, trotter_rows(st, ops, dt, order, evol), st.dim, ctx)
 
 
-def applygates(psi: GMPS, gates: GateList, cutoff=0.0, maxdim=0, mindim=1):
-    """applygates! (gatelist.jl:191-227)"""
+def lift_to_output_index(gate, d):
+    """A gate of the reference's layout (g[o', o] or g[o1', o1, o2', o2]) as
+    the same gate on fused MPO sites (index o + d*i), acting on the output
+    index and leaving the input index alone: applygate on a rank-2 GMPS
+    contracts the gate with each site's first physical index
+    (gatelist.jl:146-154 with r = 2)."""
+    eye = np.eye(d, dtype=np.complex128)
+    g = np.asarray(gate, dtype=np.complex128)
+    if g.ndim == 2:
+        return np.reshape(np.einsum("po,ab->paob", g, eye), (d * d, d * d), order="F")
+    lifted = np.einsum("pkql,ab,cd->pakbqcld", g, eye, eye)
+    return np.reshape(lifted, (d * d,) * 4, order="F")
+
+
+def applygates(psi, gates: GateList, cutoff=0.0, maxdim=0, mindim=1):
+    """applygates! (gatelist.jl:191-227) on an MPS, or on an MPO (GMPO) with
+    every gate acting on the output index."""
     t = L.trunc(cutoff, maxdim, mindim)
+    if getattr(psi, "rank", 1) == 2:
+        lifted = getattr(gates, "_lifted", None)
+        if lifted is None:
+            rows = [(sites, [lift_to_output_index(g, psi.d) for g in gs]) for sites, gs in gates.rows]
+            lifted = GateList(gates.length, rows, psi.d * psi.d, gates.ctx)
+            gates._lifted = lifted
+        psi.ctx.check(psi.ctx.lib.tn_applygates(psi.ctx.h, psi.mps._h, lifted._h, C.byref(t)))
+        return
     psi.ctx.check(psi.ctx.lib.tn_applygates(psi.ctx.h, psi._h, gates._h, C.byref(t)))
 
 

@@ -149,9 +149,12 @@ def overlap(phi, psi):
 def applyMPO(O, psi, cutoff=0.0, maxdim=0, mindim=1):
     """applyMPO(O, psi; kwargs) = MPOMPSProduct (mpo.jl:105-146): O|psi> as a
     new MPS, centred at site 1 after a truncating sweep.  An MPSProjector
-    as O applies (<left|psi>/constant) right (projector.jl:41-47)."""
+    as O applies (<left|psi>/constant) right (projector.jl:41-47); with psi an
+    MPO it is the MPO product O psi (MPOMPOProduct, mpo.jl:147-167)."""
     if isinstance(O, MPSProjector):
         return O.apply(psi)
+    if getattr(psi, "rank", 1) == 2:  # an MPO times an MPO (mpo.jl:147-167)
+        return mpo_product(O, psi, cutoff, maxdim, mindim)
     t = L.trunc(cutoff, maxdim, mindim)
     h = C.c_void_p()
     psi.ctx.check(psi.ctx.lib.tn_mpo_apply(psi.ctx.h, O._h, psi._h, C.byref(t), C.byref(h)))
@@ -211,6 +214,122 @@ class MPOHandle:
         if h and self.ctx.h:
             self.ctx.lib.tn_mpo_destroy(h)
             self._h = None
+
+
+class GMPO:
+    """Rank-2 GMPS (an MPO) on the GPU in fused form: an MPS of physical
+    dimension d^2 whose index is o + d*i, the column-major grouping of a site
+    [Dl, o, i, Dr] and the grouping the reference's rank-2 SVDs use
+    (gmps.jl:8-13, 199-267).  Gauge moves, truncated splits, norms and gate
+    rows run through the MPS machinery on that form."""
+
+    rank = 2
+
+    def __init__(self, fused: GMPS, d):
+        self.mps = fused
+        self.d = self.dim = d
+        self.N = fused.N
+        self.ctx = fused.ctx
+
+    @classmethod
+    def from_tensors(cls, tensors, center=0, ctx=None):
+        """Sites [Dl, d, d, Dr] (output index first, as the reference's)."""
+        d = tensors[0].shape[1]
+        fused = [np.reshape(L.cplx_f(t), (t.shape[0], d * d, t.shape[3]), order="F")
+                 for t in tensors]
+        return cls(GMPS.from_tensors(fused, center, ctx), d)
+
+    def __len__(self):
+        return self.N
+
+    def tensors(self):
+        d = self.d
+        return [np.reshape(t, (t.shape[0], d, d, t.shape[2]), order="F")
+                for t in self.mps.tensors()]
+
+    def __getitem__(self, i):
+        return self.tensors()[i - 1]
+
+    def bonddims(self):
+        return self.mps.bonddims()
+
+    def maxbonddim(self):
+        return self.mps.maxbonddim()
+
+    @property
+    def center(self):
+        return self.mps.center
+
+    def copy(self):
+        return GMPO(self.mps.copy(), self.d)
+
+    def movecenter(self, idx, cutoff=0.0, maxdim=0, mindim=1):
+        self.mps.movecenter(idx, cutoff, maxdim, mindim)
+
+    def norm(self):
+        """The Frobenius norm sqrt(Tr(O^dag O)) (norm on the rank-2 GMPS, gmps.jl:29-37)."""
+        return self.mps.norm()
+
+    def normalize(self):
+        self.mps.normalize()
+
+
+def productMPO(st, names, ctx=None):
+    """productMPO(st, names) (mpo.jl:85-93): a product MPO of named local
+    operators, centre unset."""
+    ts = [np.reshape(np.asarray(st.op(n), dtype=np.complex128), (1, st.dim, st.dim, 1), order="F")
+          for n in names]
+    return GMPO.from_tensors(ts, 0, ctx)
+
+
+def as_gmpo(O, ctx=None):
+    """An MPO handle (built from an OpList) or a GMPO as a GMPO."""
+    if isinstance(O, GMPO):
+        return O
+    if isinstance(O, MPOHandle):
+        return GMPO.from_tensors(O.tensors, 0, ctx or O.ctx)
+    raise TypeError("expected an MPO")
+
+
+def adjoint(O):
+    """adjoint(O) (mpo.jl:32-39): every site conjugated, physical indices swapped."""
+    O = as_gmpo(O)
+    ts = [np.conj(np.transpose(t, (0, 2, 1, 3))) for t in O.tensors()]
+    return GMPO.from_tensors(ts, O.center, O.ctx)
+
+
+def mpo_product(O1, O2, cutoff=0.0, maxdim=0, mindim=1):
+    """applyMPO(O1, O2; kwargs) = MPOMPOProduct (mpo.jl:147-167): O1 O2 as a
+    new MPO, centred at site 1 after a truncating sweep."""
+    A, B = as_gmpo(O1), as_gmpo(O2)
+    if A.d != B.d or A.N != B.N:
+        raise ValueError("GMPS must share the same physical dims and length.")
+    t = L.trunc(cutoff, maxdim, mindim)
+    h = C.c_void_p()
+    A.ctx.check(A.ctx.lib.tn_mpo_mpo_apply(A.ctx.h, A.mps._h, B.mps._h, A.d, C.byref(t),
+                                           C.byref(h)))
+    return GMPO(GMPS(h, A.N, A.d * A.d, A.ctx), A.d)
+
+
+def trace(*ops):
+    """trace(O1, ..., Ok) = Tr(O1 ... Ok) (mpo.jl:229-252): Tr(O) as the
+    overlap with the identity, Tr(A B) as <<A^dag|B>> of the fused forms, and
+    longer products through untruncated MPO products first."""
+    if not ops:
+        raise ValueError("There must be at least 1 MPO argument (rank 2).")
+    gs = [as_gmpo(o) for o in ops]
+    d, N = gs[0].d, gs[0].N
+    if any(g.d != d for g in gs):
+        raise ValueError("GMPS must share the same physical dim.")
+    if any(g.N != N for g in gs):
+        raise ValueError("GMPS must share the same length.")
+    if len(gs) == 1:
+        eye = [np.reshape(np.eye(d, dtype=np.complex128), (1, d, d, 1), order="F")] * N
+        return overlap(GMPO.from_tensors(eye, 0, gs[0].ctx).mps, gs[0].mps)
+    X = gs[0]
+    for g in gs[1:-1]:
+        X = mpo_product(X, g)
+    return overlap(adjoint(X).mps, gs[-1].mps)
 
 
 def MPO(st: Sitetypes, H, cutoff=1e-15, ctx=None):

@@ -400,3 +400,35 @@ def test_heff2_reference_order_matches_optimal_order():
     a = O.core.heff2(L, W1, W2, R, th)
     b = O.core.heff2_reference_order(L, W1, W2, R, th)
     assert np.allclose(a, b, rtol=1e-13, atol=1e-12)
+
+
+def test_mpo_algebra_and_thermal_state_match_dense():
+    """MPOMPOProduct, adjoint and trace (mpo.jl:32-39, 147-167, 229-252)
+    against dense matrices, and the thermal-state workflow of
+    examples/thermal.jl (the identity evolved by exp(-dt H) gates to beta/2,
+    energy Tr(H U^dag U) / Tr(U^dag U)) against exact diagonalisation, within
+    the second-order Trotter error at dt = 0.05."""
+    import scipy.linalg as sl
+    st = O.spinhalf()
+    N = 5
+    H = tfim(N, 1.0, 1.0)
+    W = O.mpo_from_oplist(st, H)
+    Hd = X.oplist_to_dense(st, H)
+    assert np.allclose(X.mpo_to_dense(O.mpo_mpo_product(W, W)), Hd @ Hd, atol=1e-10)
+    assert np.allclose(X.mpo_to_dense(O.adjoint_mpo(W)), Hd.conj().T, atol=1e-12)
+    assert abs(O.trace_mpos(W, W) - np.trace(Hd @ Hd)) < 1e-9
+    beta, dt = 1.0, 0.05
+    mH = O.OpList(N)
+    for ops, sites, c in zip(H.ops, H.sites, H.coeffs):
+        mH.add(ops, sites, -c)
+    rows = O.trotterize(st, mH, dt)
+    U = O.product_mpo(st, ["id"] * N)
+    for _ in range(int(round(beta / 2 / dt))):
+        O.applygates(U, rows, cutoff=1e-12, maxdim=64)
+    Ud = X.mpo_to_dense(U)
+    assert np.linalg.norm(Ud - sl.expm(-beta / 2 * Hd)) <= 2e-3 * np.linalg.norm(Ud)
+    Ua = O.adjoint_mpo(U)
+    E = O.trace_mpos(W, Ua, U) / O.trace_mpos(Ua, U)
+    ev = np.linalg.eigvalsh(Hd)
+    w = np.exp(-beta * ev)
+    assert abs(E - np.sum(w * ev) / np.sum(w)) < 1e-4
