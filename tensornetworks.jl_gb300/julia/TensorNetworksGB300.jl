@@ -262,6 +262,33 @@ function applyMPO(O::GMPS, psi::GMPS; cutoff::Real=0.0, maxdim::Int=0, mindim::I
     end
 end
 
+# MPOMPOProduct (mpo.jl:147-167) through tn_mpo_mpo_apply: each rank-2 site
+# [Dl, o, i, Dr] is uploaded as an MPS site [Dl, o + d*i, Dr] (the same
+# column-major memory), and the fused product is reshaped back.
+function fused(O::GMPS)
+    d = dim(O)
+    return GMPS(1, d^2, [reshape(O[i], size(O[i], 1), d^2, size(O[i], 4)) for i in 1:length(O)],
+                center(O))
+end
+
+function applyMPO(O1::GMPS, O2::GMPS; cutoff::Real=0.0, maxdim::Int=0, mindim::Int=1, kwargs...)
+    (rank(O1) == 2 && rank(O2) == 2) || error("applyMPO of two GMPS here takes two MPOs")
+    ctx = context()
+    d = dim(O1)
+    ha = upload(ctx, fused(O1)); hb = upload(ctx, fused(O2))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    try
+        check(ctx, ccall((:tn_mpo_mpo_apply, libtngpu), Int32,
+                         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ref{TruncOpts}, Ref{Ptr{Cvoid}}),
+                         ctx.h, ha, hb, d, TruncOpts(cutoff, maxdim, mindim), out))
+        f = new_gmps(ctx, out[], fused(O1))
+        return GMPS(2, d, [reshape(f[i], size(f[i], 1), d, d, size(f[i], 3)) for i in 1:length(f)],
+                    center(f))
+    finally
+        destroy_mps(ha); destroy_mps(hb)
+    end
+end
+
 function inner(phi::GMPS, psi::GMPS)
     ctx = context()
     ha = upload(ctx, phi); hb = upload(ctx, psi)
