@@ -77,10 +77,10 @@ def _xxz(tn, N):
 def test_dmrg_mixed_matches_fp64(tn, precision):
     """Mixed-precision DMRG (3xTF32 matvecs and projections; environments in
     3xTF32 or FP64; FP64 Lanczos and truncation) against the plain FP64 run
-    from the same state: |dE/E| <= 1e-9 on the FP64-recomputed energy.  With
-    FP64 environments the kept bond dimensions are identical; with 3xTF32
-    environments they may differ by a few where sigma^2 sits at the 1e-12
-    cutoff (mixed products perturb the state at ~1e-7)."""
+    from the same state: |dE/E| <= 1e-9 on the FP64-recomputed energy.  Kept
+    bond dimensions set by the 1e-12 cutoff may differ by a few where sigma^2
+    sits at the cutoff: the 3xTF32 H_eff products perturb the state at ~1e-7
+    in both modes."""
     N, D = 24, 8
     rng = np.random.default_rng(3)
     shapes = [((1 if i == 0 else D), 2, (1 if i == N - 1 else D)) for i in range(N)]
@@ -98,10 +98,7 @@ def test_dmrg_mixed_matches_fp64(tn, precision):
     _, Emx = tn.dmrg(pmx, W, precision=precision, stats=st, **kw)
     assert abs(st["energy_fp64"] - E64) <= 1e-9 * abs(E64), (st["energy_fp64"], E64, Emx)
     assert Emx == st["energy_fp64"]  # mixed modes return the FP64 Rayleigh quotient
-    if precision == "mixed-env64":
-        assert pmx.bonddims() == p64.bonddims()
-    else:
-        assert abs(max(pmx.bonddims()) - max(p64.bonddims())) <= 4
+    assert abs(max(pmx.bonddims()) - max(p64.bonddims())) <= 4
 
 
 @pytest.mark.parametrize("cl,cr,wl,wr", [(1, 2, 1, 5), (9, 17, 5, 5), (64, 96, 5, 5), (300, 256, 5, 3)])
