@@ -71,6 +71,9 @@ def parse():
                    help="qjmc: start every trajectory from one trajectory evolved this many "
                         "steps (untimed) instead of the all-up state")
     p.add_argument("--tebd-steps", type=int, default=60, help="tebd: steps of the quench")
+    p.add_argument("--tebd-random-chi", type=int, default=0,
+                   help="tebd: start from a seeded random MPS of this bond dimension instead of "
+                        "the Neel state (a profiling case at the saturated bond dimension)")
     p.add_argument("--segments", type=int, default=100, help="tebd-grad: h segments")
     p.add_argument("--fd-coords", type=int, default=2,
                    help="tebd-grad: coordinates checked by central differences")
@@ -763,6 +766,27 @@ def qjmc_run(args):
     print(json.dumps(line))
 
 
+def tebd_step_flops(dims0, dims1, d=2):
+    """Algorithmic FP64 flops of one TEBD step on an N-site chain, counted
+    per bond with the larger of the bond dimensions before and after the
+    step: each bond takes a two-site gate split and a truncating centre move
+    in the 2nd-order schedule's three rows (1.5 gate applications and about
+    as many moves per bond): the two-site tensor (8 Dl d^2 Dr Dm), the gate
+    leg (8 Dl Dr d^4), the Gram matrix of order n = d D (4 n^2 (n + 1)),
+    the eigensolve (16/3 n^3 + 8 n^2 k) and the projection (8 n^2 k)."""
+    total = 0.0
+    N = len(dims0) - 1
+    for b in range(1, N):
+        D = max(dims0[b], dims1[b])
+        Dl = max(dims0[b - 1], dims1[b - 1])
+        Dr = max(dims0[b + 1], dims1[b + 1])
+        n, k = d * max(Dl, Dr), D
+        split = 4.0 * n * n * (n + 1) + 16.0 / 3.0 * n ** 3 + 8.0 * n * n * k + 8.0 * n * n * k
+        gate = 8.0 * Dl * d * d * Dr * D + 8.0 * Dl * Dr * d ** 4
+        total += 1.5 * (gate + split) + 1.5 * split
+    return total
+
+
 def tebd_run(args):
     """TEBD quench: N=64 XXZ (J=1, Delta=0.5) + 0.2(-1)^i Z_i, Neel start, real
     time, 2nd order, dt=0.05, maxdim 256, cutoff 1e-10, <Z_i> and S(N/2) after
@@ -789,31 +813,72 @@ def tebd_run(args):
     rec = {}
     clk = Clocks(0)
     for prec in ("fp64", "mixed"):
-        psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
+        if args.tebd_random_chi:
+            import oracle as Ocpu  # the seeded initial tensors only
+            po = Ocpu.random_mps(2, N, args.tebd_random_chi, np.random.default_rng(7))
+            psi = tn.GMPS.from_tensors(po.tensors, po.center, ctx)
+        else:
+            psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
         psi.norm()
-        zs, ss, step_s = [], [], 0.0
+        zs, ss, step_s, flops = [], [], 0.0, 0.0
         ln = C.c_double(0.0)
         for _ in range(steps):
+            dims0 = psi.bonddims()
             t0 = time.perf_counter()
             ctx.check(ctx.lib.tn_tebd_steps_prec(ctx.h, psi._h, gates._h, 1, C.byref(t),
                                                  L.PREC[prec], C.byref(ln)))
             step_s += time.perf_counter() - t0
+            flops += tebd_step_flops(dims0, psi.bonddims())
             zs.append(np.real(tn.inner(st, psi, Z, psi)))
             ss.append(psi.entropy(N // 2))
         rec[prec] = {"steps_per_s": steps / step_s, "chi_end": psi.maxbonddim(),
-                     "z": np.asarray(zs), "s": np.asarray(ss)}
+                     "z": np.asarray(zs), "s": np.asarray(ss), "flops": flops, "seconds": step_s}
+        if prec == "fp64":
+            final = psi.tensors(), psi.center
         log(f"tebd {prec}: {steps / step_s:.3f} steps/s, chi_end {psi.maxbonddim()}")
     clocks = clk.stop()
+    fp64_peak = cublas_zgemm_tflops(ctx.device)
+    achieved = rec["fp64"]["flops"] / rec["fp64"]["seconds"] / 1e12
+    cpu = None
+    if not args.no_cpu:
+        # one step of the numpy restatement from the FP64 run's final state
+        import oracle as Ocpu
+        Ho = Ocpu.OpList(N)
+        for ops, sites, c in zip(H.ops, H.sites, H.coeffs):
+            Ho.add(ops, sites, c)
+        rows = Ocpu.trotterize(Ocpu.spinhalf(), Ho, dt, order=2, evol="real")
+        po = Ocpu.GMPS(1, 2, final[0], final[1])
+        t0 = time.perf_counter()
+        Ocpu.applygates(po, rows, cutoff=1e-10, maxdim=256)
+        cs = time.perf_counter() - t0
+        cpu = {"value": 1.0 / cs, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+               "blas_threads": blas_threads(),
+               "sample": f"one TEBD step of the numpy restatement from the FP64 run's final "
+                         f"state (chi {max(b for b in po.bonddims())}), {cs:.1f} s"}
+        log(f"tebd cpu: {cpu}")
     dz = float(np.max(np.abs(rec["mixed"]["z"] - rec["fp64"]["z"])))
     ds = float(np.max(np.abs(rec["mixed"]["s"] - rec["fp64"]["s"])))
     line = {"metric": "TEBD steps/s", "value": rec["fp64"]["steps_per_s"], "unit": "steps/s",
             "n_gpus": 1, "higher_is_better": True, "dtype": "c128 (f64)", "data": "synthetic",
-            "config": {"workload": f"N=64 XXZ J=1 Delta=0.5 + 0.2(-1)^i Z_i, Neel, dt=0.05, "
-                                   f"{steps} steps (t={steps * dt:.2f}), maxdim 256, cutoff 1e-10"},
+            "config": {"workload": f"N=64 XXZ J=1 Delta=0.5 + 0.2(-1)^i Z_i, "
+                                   + (f"random MPS D={args.tebd_random_chi} (profiling case)"
+                                      if args.tebd_random_chi else "Neel")
+                                   + f", dt=0.05, {steps} steps (t={steps * dt:.2f}), maxdim 256, "
+                                     "cutoff 1e-10"},
             "mixed_steps_per_s": rec["mixed"]["steps_per_s"],
             "chi_end": {k: v["chi_end"] for k, v in rec.items()},
             "mixed_vs_fp64_max_abs_dZ": dz, "mixed_vs_fp64_max_abs_dS": ds,
             "fp64_final_S_half": float(rec["fp64"]["s"][-1]), "clocks": clocks,
+            "roofline": {"kernel": "whole TEBD step (latency-bound: one grid eigensolver per "
+                                   "split)", "bound": "fp64-pipe", "achieved": achieved,
+                         "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak if fp64_peak else None,
+                         "note": "algorithmic FP64 flops of the FP64 run's steps (two-site "
+                                 "tensor, gate leg, Gram matrix, the LAPACK count of the "
+                                 "eigensolve, projection, for every gate and every truncating "
+                                 "centre move, at the bond dimensions before and after each "
+                                 "step) over the step time"},
+            "cpu_baseline": cpu,
             "note": "steps/s counts the gate layers and the normalisation (tn_tebd_steps_prec); "
                     "observables are measured between steps, outside the timing"}
     print(json.dumps(line))
