@@ -814,9 +814,7 @@ def tebd_run(args):
     clk = Clocks(0)
     for prec in ("fp64", "mixed"):
         if args.tebd_random_chi:
-            import oracle as Ocpu  # the seeded initial tensors only
-            po = Ocpu.random_mps(2, N, args.tebd_random_chi, np.random.default_rng(7))
-            psi = tn.GMPS.from_tensors(po.tensors, po.center, ctx)
+            psi = tn.randomMPS(2, N, args.tebd_random_chi, rng=np.random.default_rng(7), ctx=ctx)
         else:
             psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
         psi.norm()
