@@ -70,7 +70,7 @@ struct Ctx {
     int sm_count = 0;
     // reusable scratch for the hot path
     Scratch s_gram, s_eigval, s_work, s_x, s_y, s_t1, s_t2, s_dot, s_coef, s_mixa, s_mixb, s_mixc,
-        s_mixd, s_mixe, s_mixf, s_eig;
+        s_mixd, s_mixe, s_mixf, s_eig, s_splitk;
     int* d_info = nullptr;
     // grid-barrier words of the eigensolver's cooperative kernels: arrival
     // count, generation, and an error word set when a bounded wait ran out
@@ -79,6 +79,9 @@ struct Ctx {
     // mixed precision on: environment updates and truncation projections run
     // on the tensor cores (set for the duration of a mixed-precision sweep)
     bool mixed = false;
+    // split-K FP64 GEMMs draw partial buffers from the pool; callers that must
+    // not allocate turn them off
+    bool splitk = true;
     double* h_pinned = nullptr;  // small pinned staging area
     size_t h_pinned_n = 0;
     // kernel profiler: CUDA events around launches, per class

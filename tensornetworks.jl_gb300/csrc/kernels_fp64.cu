@@ -21,15 +21,19 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
                                                     int64_t sA, const cplx* __restrict__ B,
                                                     int64_t ldb, int64_t sB, cplx beta,
                                                     cplx* __restrict__ C, int64_t ldc, int64_t sC,
-                                                    int lower) {
+                                                    int lower, int64_t kc) {
     __shared__ cplx As[GB_K][GB_M + 1];
     __shared__ cplx Bs[GB_K][GB_N + 1];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    const int64_t bz = blockIdx.z;
+    // kc > 0: split K; blockIdx.z is the chunk and C the chunk's partial
+    // (M x N, ld M); otherwise blockIdx.z is the batch index
+    const int64_t bz = kc > 0 ? 0 : blockIdx.z;
+    const int64_t k_lo = kc > 0 ? (int64_t)blockIdx.z * kc : 0;
+    const int64_t k_hi = kc > 0 ? min(K, k_lo + kc) : K;
     A += bz * sA;
     B += bz * sB;
-    C += bz * sC;
+    C += kc > 0 ? (int64_t)blockIdx.z * M * N : bz * sC;
     const int64_t m0 = (int64_t)blockIdx.x * GB_M, n0 = (int64_t)blockIdx.y * GB_N;
     // lower: only the lower triangle is wanted (a Hermitian Gram matrix read
     // by the eigensolver, which reads the lower triangle); tiles strictly
@@ -41,7 +45,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
 
-    for (int64_t k0 = 0; k0 < K; k0 += GB_K) {
+    for (int64_t k0 = k_lo; k0 < k_hi; k0 += GB_K) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             int mm, kk;
@@ -54,7 +58,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
             }
             const int64_t gm = m0 + mm, gk = k0 + kk;
             cplx v = cmk(0.0, 0.0);
-            if (gm < M && gk < K) {
+            if (gm < M && gk < k_hi) {
                 v = (OPA == OP_N || OPA == OP_R) ? A[gm + gk * lda] : A[gk + gm * lda];
                 if (OPA == OP_C || OPA == OP_R) v.y = -v.y;
             }
@@ -72,7 +76,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int64_t M, int64_t N, int64_
             }
             const int64_t gn = n0 + nn, gk = k0 + kk;
             cplx v = cmk(0.0, 0.0);
-            if (gn < N && gk < K) {
+            if (gn < N && gk < k_hi) {
                 v = (OPB == OP_N || OPB == OP_R) ? B[gk + gn * ldb] : B[gn + gk * ldb];
                 if (OPB == OP_C || OPB == OP_R) v.y = -v.y;
             }
@@ -142,6 +146,25 @@ __global__ void __launch_bounds__(64) zgemm_small_kernel(int64_t M, int64_t N, i
     }
 }
 
+// C = alpha sum_z P[z] + beta C over the split-K partials in chunk order
+// (deterministic); lower: entries above the diagonal are left alone.
+__global__ void splitk_reduce_kernel(const cplx* __restrict__ P, int64_t M, int64_t N, int S,
+                                     cplx alpha, cplx beta, cplx* __restrict__ C, int64_t ldc,
+                                     int lower) {
+    const int64_t total = M * N;
+    const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % M, j = e / M;
+        if (lower && i < j) continue;
+        cplx acc = cmk(0, 0);
+        for (int z = 0; z < S; ++z) acc = cadd(acc, P[e + (int64_t)z * total]);
+        cplx v = cmul(alpha, acc);
+        if (use_beta) v = cfma(beta, C[i + j * ldc], v);
+        C[i + j * ldc] = v;
+    }
+}
+
 template <int OPA>
 void zgemm_small_dispatch_b(Ctx* ctx, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha,
                             const cplx* A, int64_t lda, int64_t sA, const cplx* B, int64_t ldb,
@@ -161,19 +184,20 @@ void zgemm_small_dispatch_b(Ctx* ctx, Op opb, int64_t m, int64_t n, int64_t k, c
 template <int OPA>
 void zgemm_dispatch_b(Ctx* ctx, Op opb, dim3 grid, int64_t m, int64_t n, int64_t k, cplx alpha,
                       const cplx* A, int64_t lda, int64_t sA, const cplx* B, int64_t ldb,
-                      int64_t sB, cplx beta, cplx* C, int64_t ldc, int64_t sC, int lower) {
+                      int64_t sB, cplx beta, cplx* C, int64_t ldc, int64_t sC, int lower,
+                      int64_t kc) {
     switch (opb) {
         case OP_N:
-            zgemm_kernel<OPA, OP_N><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
+            zgemm_kernel<OPA, OP_N><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, kc);
             break;
         case OP_T:
-            zgemm_kernel<OPA, OP_T><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
+            zgemm_kernel<OPA, OP_T><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, kc);
             break;
         case OP_C:
-            zgemm_kernel<OPA, OP_C><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
+            zgemm_kernel<OPA, OP_C><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, kc);
             break;
         case OP_R:
-            zgemm_kernel<OPA, OP_R><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower);
+            zgemm_kernel<OPA, OP_R><<<grid, 256, 0, ctx->stream>>>(m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, kc);
             break;
     }
 }
@@ -543,11 +567,39 @@ void zgemm(Ctx* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplx alpha
         TN_CHECK_CUDA(cudaGetLastError());
         return;
     }
+    // Split K when the tiles cannot fill the SMs (the Gram and projection
+    // products of bond dimensions 128-512): S chunks of at least 128, each
+    // into its own partial, summed in chunk order by a second kernel.
+    const int64_t tiles = (int64_t)grid.x * grid.y;
+    int64_t S = 1;
+    if (ctx->splitk && batch == 1 && k >= 512 && tiles < ctx->sm_count)
+        S = std::min<int64_t>((2 * ctx->sm_count + tiles - 1) / tiles, k / 128);
+    if (S > 1) {
+        const int64_t kc = ((k + S - 1) / S + GB_K - 1) / GB_K * GB_K;
+        S = (k + kc - 1) / kc;
+        cplx* P = ctx->s_splitk.c(ctx, (size_t)(S * m * n));
+        dim3 g2(grid.x, grid.y, (unsigned)S);
+        const cplx one = cmk(1, 0), zero = cmk(0, 0);
+        switch (opa) {
+            case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, g2, m, n, k, one, A, lda, 0, B, ldb, 0, zero, P, m, 0, lower, kc); break;
+            case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, g2, m, n, k, one, A, lda, 0, B, ldb, 0, zero, P, m, 0, lower, kc); break;
+            case OP_C: zgemm_dispatch_b<OP_C>(ctx, opb, g2, m, n, k, one, A, lda, 0, B, ldb, 0, zero, P, m, 0, lower, kc); break;
+            case OP_R: zgemm_dispatch_b<OP_R>(ctx, opb, g2, m, n, k, one, A, lda, 0, B, ldb, 0, zero, P, m, 0, lower, kc); break;
+        }
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+        const int64_t blocks = std::min<int64_t>((m * n + 255) / 256, (int64_t)ctx->sm_count * 8);
+        splitk_reduce_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(P, m, n, (int)S, alpha, beta,
+                                                                        C, ldc, lower);
+        ctx->count();
+        TN_CHECK_CUDA(cudaGetLastError());
+        return;
+    }
     switch (opa) {
-        case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
-        case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
-        case OP_C: zgemm_dispatch_b<OP_C>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
-        case OP_R: zgemm_dispatch_b<OP_R>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower); break;
+        case OP_N: zgemm_dispatch_b<OP_N>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, 0); break;
+        case OP_T: zgemm_dispatch_b<OP_T>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, 0); break;
+        case OP_C: zgemm_dispatch_b<OP_C>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, 0); break;
+        case OP_R: zgemm_dispatch_b<OP_R>(ctx, opb, grid, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, lower, 0); break;
     }
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());

@@ -84,7 +84,7 @@ void ctx_release(Ctx& c) {
     // scratch buffers release through the stream before it goes away
     Scratch* all[] = {&c.s_gram, &c.s_eigval, &c.s_work, &c.s_x, &c.s_y, &c.s_t1, &c.s_t2,
                       &c.s_dot, &c.s_coef, &c.s_mixa, &c.s_mixb, &c.s_mixc, &c.s_mixd, &c.s_mixe,
-                      &c.s_mixf, &c.s_eig};
+                      &c.s_mixf, &c.s_eig, &c.s_splitk};
     for (Scratch* s : all) s->buf.reset();
     if (c.stream) cudaStreamSynchronize(c.stream);
     if (c.d_info) cudaFree(c.d_info);

@@ -118,6 +118,13 @@ void heff2_noalloc(Ctx* ctx, int64_t cl, int64_t cr, int d, int64_t wl, int64_t 
     ctx->count();
     TN_CHECK_CUDA(cudaGetLastError());
     const cplx one = cmk(1, 0), zero = cmk(0, 0);
+    // the GEMMs run unsplit: split-K partials would come from the pool
+    struct NoSplit {
+        Ctx* c;
+        bool old;
+        ~NoSplit() { c->splitk = old; }
+    } guard{ctx, ctx->splitk};
+    ctx->splitk = false;
     // T1[(a w), (s1 s2 c)] = L[(a w), b] theta[b, (s1 s2 c)]
     zgemm(ctx, OP_N, OP_N, cl * wl, d2 * cr, cl, one, L, cl * wl, 0, theta, cl, 0, zero, T1, cl * wl, 0);
     // T2[a, (s1' s2' w''), c] = sum W12 T1

@@ -132,10 +132,12 @@ def test_truncate_keep_rule_and_factors(tn, case, direction):
 
 
 @pytest.mark.parametrize("direction", [0, 1])
-@pytest.mark.parametrize("m,n", [(150, 300), (300, 150)])
+@pytest.mark.parametrize("m,n", [(150, 300), (300, 150), (256, 640), (640, 256)])
 def test_truncate_rectangular_top_k(tn, m, n, direction):
     """Rectangular splits on the top-eigenpair path: the Gram order is the
-    isometric side (m or n) and exceeds the kept count."""
+    isometric side (m or n) and exceeds the kept count.  The 256 x 640 shapes
+    put a Gram product with inner dimension 640 on a grid of 4 x 4 tiles,
+    which splits K (partials summed in chunk order)."""
     ctx = tn.context()
     rng = np.random.default_rng(m + 2 * n + direction)
     S = np.geomspace(1, 1e-9, min(m, n))
