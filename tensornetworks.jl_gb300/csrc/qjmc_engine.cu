@@ -1201,7 +1201,17 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
     const int64_t mps_slot = (off + 15) / 16 * 16;
     Scr dummy;
     const int64_t scr_slot = (int64_t)scr_layout(nullptr, gmax, N, d, dummy);
-    const int slots = (int)std::min<int64_t>(ntraj, (int64_t)ctx->sm_count * blocks_per_sm);
+    int slots = (int)std::min<int64_t>(ntraj, (int64_t)ctx->sm_count * blocks_per_sm);
+    {
+        // slots beyond what fits in 80 % of the free device memory run as
+        // later waves of the same blocks instead
+        size_t free_b = 0, total_b = 0;
+        TN_CHECK_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const double per_slot = (double)sizeof(cplx) * mps_slot + (double)scr_slot;
+        const int64_t fit = (int64_t)(0.8 * (double)free_b / per_slot);
+        TN_REQUIRE(fit >= 1, "one trajectory slot does not fit in the free device memory");
+        slots = (int)std::min<int64_t>(slots, fit);
+    }
     const int nrows_out = nsteps / save_every + 1;
 
     // gates
