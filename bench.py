@@ -71,9 +71,6 @@ def parse():
                    help="qjmc: start every trajectory from one trajectory evolved this many "
                         "steps (untimed) instead of the all-up state")
     p.add_argument("--tebd-steps", type=int, default=60, help="tebd: steps of the quench")
-    p.add_argument("--tebd-random-chi", type=int, default=0,
-                   help="tebd: start from a seeded random MPS of this bond dimension instead of "
-                        "the Neel state (a profiling case at the saturated bond dimension)")
     p.add_argument("--segments", type=int, default=100, help="tebd-grad: h segments")
     p.add_argument("--fd-coords", type=int, default=2,
                    help="tebd-grad: coordinates checked by central differences")
@@ -813,10 +810,7 @@ def tebd_run(args):
     rec = {}
     clk = Clocks(0)
     for prec in ("fp64", "mixed"):
-        if args.tebd_random_chi:
-            psi = tn.randomMPS(2, N, args.tebd_random_chi, rng=np.random.default_rng(7), ctx=ctx)
-        else:
-            psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
+        psi = tn.productMPS(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)], ctx=ctx)
         psi.norm()
         zs, ss, step_s, flops = [], [], 0.0, 0.0
         ln = C.c_double(0.0)
@@ -858,11 +852,8 @@ def tebd_run(args):
     ds = float(np.max(np.abs(rec["mixed"]["s"] - rec["fp64"]["s"])))
     line = {"metric": "TEBD steps/s", "value": rec["fp64"]["steps_per_s"], "unit": "steps/s",
             "n_gpus": 1, "higher_is_better": True, "dtype": "c128 (f64)", "data": "synthetic",
-            "config": {"workload": f"N=64 XXZ J=1 Delta=0.5 + 0.2(-1)^i Z_i, "
-                                   + (f"random MPS D={args.tebd_random_chi} (profiling case)"
-                                      if args.tebd_random_chi else "Neel")
-                                   + f", dt=0.05, {steps} steps (t={steps * dt:.2f}), maxdim 256, "
-                                     "cutoff 1e-10"},
+            "config": {"workload": f"N=64 XXZ J=1 Delta=0.5 + 0.2(-1)^i Z_i, Neel, dt=0.05, "
+                                   f"{steps} steps (t={steps * dt:.2f}), maxdim 256, cutoff 1e-10"},
             "mixed_steps_per_s": rec["mixed"]["steps_per_s"],
             "chi_end": {k: v["chi_end"] for k, v in rec.items()},
             "mixed_vs_fp64_max_abs_dZ": dz, "mixed_vs_fp64_max_abs_dS": ds,
