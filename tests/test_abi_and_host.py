@@ -178,3 +178,28 @@ def test_philox_stream_matches_oracle():
                 b = trajectory_uniforms(seed, traj, n)
                 assert np.array_equal(a, b)
                 assert np.all((a >= 0.0) & (a < 1.0))
+
+
+def test_output_index_gate_lift():
+    """A gate lifted to fused MPO sites (index o + d*i) acts as the gate on
+    each site's output index and as the identity on the input index
+    (gatelist.jl:146-154 with rank 2), for one- and two-site gates."""
+    from tngpu.algorithms import lift_to_output_index
+    rng = np.random.default_rng(8)
+    d = 2
+    g1 = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+    g2 = rng.standard_normal((d,) * 4) + 1j * rng.standard_normal((d,) * 4)
+    A = rng.standard_normal((3, d, d, 4)) + 1j * rng.standard_normal((3, d, d, 4))
+    # one site: [a, o, i, b] -> sum_o' g[o, o'] A[a, o', i, b]
+    ref = np.einsum("po,aoib->apib", g1, A)
+    L1 = lift_to_output_index(g1, d)
+    Af = np.reshape(A, (3, d * d, 4), order="F")
+    got = np.einsum("PQ,aQb->aPb", L1, Af)
+    assert np.allclose(np.reshape(got, (3, d, d, 4), order="F"), ref)
+    # two sites: theta [a, o1, i1, o2, i2, b]
+    th = rng.standard_normal((3, d, d, d, d, 4)) + 1j * rng.standard_normal((3, d, d, d, d, 4))
+    ref2 = np.einsum("pkql,akilmb->apiqmb", g2, th)
+    L2 = lift_to_output_index(g2, d)
+    thf = np.reshape(th, (3, d * d, d * d, 4), order="F")
+    got2 = np.einsum("PKQL,aKLb->aPQb", L2, thf)
+    assert np.allclose(np.reshape(got2, (3, d, d, d, d, 4), order="F"), ref2)
