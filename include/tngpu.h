@@ -254,9 +254,11 @@ int32_t tn_tebd_grad(tn_ctx* ctx, const tn_mps* psi0, int32_t ngates, const tn_g
  * (qjmc.jl:170-220); ops are d x d interleaved, coeffs complex. */
 int32_t tn_qjmc_rates(tn_ctx* ctx, tn_mps* psi, int32_t njump, const int32_t* sites,
                       const double* ops, const double* coeffs, double* rates);
-/* One trajectory of qjmc_simulation with classical=true (qjmc.jl:28-166).
- * draws: the uniform stream, consumed in the reference's order (one unused
- * draw per step, one for the jump decision, one more on a jump).
+/* One trajectory of qjmc_simulation (qjmc.jl:28-166).  classical != 0: the
+ * escape-rate unraveling (the reference's default: one unused draw per step,
+ * one for the jump decision, one more on a jump); classical == 0: the jump
+ * decision compares the step's first draw with the squared norm of the
+ * unnormalised state (qjmc.jl:65-86: one draw per step, one more on a jump).
  * Observables (single-site ops) are evaluated at t=0 and every save_every
  * steps into obs_out[(nsave_rows) x nobs] (re, im).  Jump indices are
  * 1-based.  *njumps in: capacity, out: count; *ndraws_used out. */
@@ -265,7 +267,8 @@ int32_t tn_qjmc_run(tn_ctx* ctx, tn_mps* psi, const tn_gates* gates, int32_t nju
                     int32_t nsteps, double dt, const double* draws, int64_t ndraws,
                     const tn_trunc_opts* trunc, int32_t save_every, int32_t nobs,
                     const int32_t* obs_sites, const double* obs_ops, double* obs_out,
-                    int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used);
+                    int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used,
+                    int32_t classical);
 
 /* ntraj independent trajectories of the run above from the same initial MPS,
  * advanced concurrently by nworkers host threads, each with its own CUDA
@@ -300,8 +303,9 @@ int32_t tn_qjmc_batch(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, in
  * algorithmic FP64 flops of all trajectories (contractions, Gram products,
  * the LAPACK count 16/3 n^3 + 8 n^2 k of each eigensolve), the launch's
  * device time in ms (CUDA events on the context's stream), the
- * trajectory-steps and the blocks launched.  Replaces the loop of
- * qjmc_simulation calls (qjmc.jl:28-166) over an ensemble. */
+ * trajectory-steps and the blocks launched.  classical as in tn_qjmc_run.
+ * Replaces the loop of qjmc_simulation calls (qjmc.jl:28-166) over an
+ * ensemble. */
 int32_t tn_qjmc_ensemble(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates, int32_t njump,
                          const int32_t* jump_sites, const double* jump_ops,
                          const double* jump_coeffs, int32_t nsteps, double dt, int32_t ntraj,
@@ -310,7 +314,7 @@ int32_t tn_qjmc_ensemble(tn_ctx* ctx, const tn_mps* psi0, const tn_gates* gates,
                          int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
                          double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
                          int32_t* jumps, double* jumptimes, int32_t blocks_per_sm,
-                         double* stats);
+                         double* stats, int32_t classical);
 /* The per-trajectory uniform stream of tn_qjmc_batch: out[k] in [0, 1) is the
  * top 53 bits of 64-bit word k % 2 of Philox4x32-10 (Salmon et al., SC 2011)
  * at counter (k / 2 low 32 bits, trajectory, k / 2 high 32 bits, 0) under the

@@ -22,7 +22,7 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
                     const double* jops, const double* jcoeffs, int nsteps, double dt,
                     const double* draws, int64_t ndraws, const Trunc& t, int save_every,
                     int nobs, const int* obs_sites, const double* obs_ops, double* obs_out,
-                    int max_jumps);
+                    int max_jumps, bool classical);
 void mixed_unit_heff2(Ctx* ctx, const cplx* L, const cplx* W12, const cplx* R, int64_t cl,
                       int64_t cr, int d, int64_t wl, int64_t wr, const cplx* x, cplx* y);
 void mixed_gemm(Ctx* ctx, int64_t m, int64_t n, int64_t k, const cplx* A, bool conj_a,
@@ -40,7 +40,8 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
                    const double* draws, int64_t ndraws_per_traj, uint64_t seed, uint32_t first_traj,
                    const Trunc& t, int save_every, int nobs, const int* obs_sites,
                    const double* obs_ops, double* obs_avg, int* njumps_per_traj, int max_jumps,
-                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats);
+                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats,
+                   bool classical);
 void philox_uniforms(uint64_t seed, uint32_t traj, int64_t n, double* out);
 struct VmpsResult {
     double cost;
@@ -699,13 +700,14 @@ int32_t tn_qjmc_run(tn_ctx* h, tn_mps* psi, const tn_gates* g, int32_t njump,
                     int32_t nsteps, double dt, const double* draws, int64_t ndraws,
                     const tn_trunc_opts* t, int32_t save_every, int32_t nobs,
                     const int32_t* obs_sites, const double* obs_ops, double* obs_out,
-                    int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used) {
+                    int32_t* jumps, double* jumptimes, int32_t* njumps, int64_t* ndraws_used,
+                    int32_t classical) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(psi && g && njumps && (ndraws == 0 || draws), "null argument");
     TN_REQUIRE(nsteps >= 0 && njump >= 1, "need at least one jump operator");
     QjmcResult r = qjmc_run(psi, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, draws,
                             ndraws, to_trunc(t), save_every, nobs, obs_sites, obs_ops, obs_out,
-                            *njumps);
+                            *njumps, classical != 0);
     for (size_t i = 0; i < r.jumps.size(); ++i) {
         jumps[i] = r.jumps[i];
         jumptimes[i] = r.times[i];
@@ -740,14 +742,14 @@ int32_t tn_qjmc_ensemble(tn_ctx* h, const tn_mps* psi0, const tn_gates* g, int32
                          int32_t nobs, const int32_t* obs_sites, const double* obs_ops,
                          double* obs_avg, int32_t* njumps_per_traj, int32_t max_jumps,
                          int32_t* jumps, double* jumptimes, int32_t blocks_per_sm,
-                         double* stats) {
+                         double* stats, int32_t classical) {
     TN_API_BEGIN(h ? &h->c : nullptr)
     TN_REQUIRE(psi0 && g && obs_avg && jump_sites && jump_ops && jump_coeffs, "null argument");
     TN_REQUIRE(nobs == 0 || (obs_sites && obs_ops), "null observables");
     qjmc_ensemble(psi0, g, njump, jump_sites, jump_ops, jump_coeffs, nsteps, dt, ntraj, draws,
                   ndraws_per_traj, seed, first_traj, to_trunc(t), save_every, nobs, obs_sites,
                   obs_ops, obs_avg, njumps_per_traj, max_jumps, jumps, jumptimes, blocks_per_sm,
-                  stats);
+                  stats, classical != 0);
     TN_API_END
 }
 

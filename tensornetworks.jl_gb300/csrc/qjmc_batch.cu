@@ -25,7 +25,7 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
                     const double* jops, const double* jcoeffs, int nsteps, double dt,
                     const double* draws, int64_t ndraws, const Trunc& t, int save_every,
                     int nobs, const int* obs_sites, const double* obs_ops, double* obs_out,
-                    int max_jumps);
+                    int max_jumps, bool classical);
 
 // The uniform stream of trajectory `traj` under `seed`: draw k in [0, 1)
 // from the 64-bit word (k % 2) of Philox4x32-10(counter = (k / 2 low, traj,
@@ -83,7 +83,7 @@ void qjmc_batch(const tn_mps* psi0, const tn_gates* g, int njump, const int* jsi
                 QjmcResult r = qjmc_run(&psi, g, njump, jsites, jops, jcoeffs, nsteps, dt,
                                         dr, ndraws_per_traj, t,
                                         save_every, nobs, obs_sites, obs_ops, buf.data(),
-                                        nsteps + 1);
+                                        nsteps + 1, true);
                 for (size_t k = 0; k < nout; ++k) local[k] += buf[k];
                 if (njumps_per_traj) njumps_per_traj[tr] = (int)r.jumps.size();
             }

@@ -46,6 +46,7 @@ enum : int { QE_OK = 0, QE_CAPACITY = 1, QE_DRAWS = 2, QE_JUMPS = 3, QE_NOCHANNE
 
 struct QjParams {
     int N, d, nsteps, save_every, nobs, njump, maxj, nrows_out;
+    int classical;  // 0: jump decision from the norm lost in the step (qjmc.jl:65-86)
     double dt, cutoff;
     int maxdim, mindim;
     int nrows;  // gate rows
@@ -851,7 +852,8 @@ __device__ void applygates(Traj& T) {
     }
 }
 
-__device__ __noinline__ void normalize(Traj& T) {
+// Normalises the centre tensor; returns the squared norm before scaling.
+__device__ __noinline__ double normalize(Traj& T) {
     Sh& sh = *T.sh;
     if (sh.center == 0) movecenter(T, 1, TruncD{0.0, 0, 1});
     const int c = sh.center, n = T.dl(c) * T.p->d * T.dr(c);
@@ -862,6 +864,7 @@ __device__ __noinline__ void normalize(Traj& T) {
     const double inv = 1.0 / sqrt(n2);
     for (int e = threadIdx.x; e < n; e += QT) A[e] = cmk(A[e].x * inv, A[e].y * inv);
     __syncthreads();
+    return n2;
 }
 
 // rho[s + D s'] = sum_{a,b} conj(A[a,s,b]) Y[a,s',b] (A, Y: Dl x D x Dr); the
@@ -1041,22 +1044,34 @@ __device__ void run_traj(const QjParams& p, Sh& sh, int t, int slot) {
         applygates(T);
         if (sh.flag) break;
         double u;
-        if (!draw(T, u)) {  // qjmc.jl:64 draws once per step; unused when classical
+        if (!draw(T, u)) {  // qjmc.jl:64; the jump decision when not classical
             set_flag(sh, QE_DRAWS);
             break;
         }
-        normalize(T);
+        const double n2 = normalize(T);
         if (sh.flag) break;
-        rho_all(T);
+        bool want = false, rho_fresh = false;
         double er = 0.0;
-        for (int j = 0; j < p.njump; ++j) er += rate(T, j);
-        const double prob = exp(-er * p.dt);
-        if (!draw(T, u)) {
-            set_flag(sh, QE_DRAWS);
-            break;
+        if (p.classical) {
+            rho_all(T);
+            rho_fresh = true;
+            for (int j = 0; j < p.njump; ++j) er += rate(T, j);
+            const double prob = exp(-er * p.dt);
+            double u2;
+            if (!draw(T, u2)) {
+                set_flag(sh, QE_DRAWS);
+                break;
+            }
+            want = u2 > prob;
+        } else {
+            want = u > n2;  // the squared norm of the unnormalised state
+            if (want) {
+                rho_all(T);
+                rho_fresh = true;
+                for (int j = 0; j < p.njump; ++j) er += rate(T, j);
+            }
         }
-        bool jumped = false;
-        if (u > prob) {
+        if (want) {
             double r;
             if (!draw(T, r)) {
                 set_flag(sh, QE_DRAWS);
@@ -1092,11 +1107,11 @@ __device__ void run_traj(const QjParams& p, Sh& sh, int t, int slot) {
                 p.jump_time[(size_t)t * p.maxj + nj] = time + p.dt;
             }
             ++nj;
-            jumped = true;
+            rho_fresh = false;
         }
         time += p.dt;
         if (step % p.save_every == 0 && p.nobs > 0) {
-            if (jumped) rho_all(T);
+            if (!rho_fresh) rho_all(T);
             for (int k = threadIdx.x; k < p.nobs; k += QT)
                 p.obs_traj[((size_t)t * p.nrows_out + row) * p.nobs + k] =
                     expect(T.s.rho + (size_t)(p.osite[k] - 1) * d * d, p.oO + (size_t)k * d * d, d);
@@ -1162,7 +1177,8 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
                    const double* draws, int64_t ndraws_per_traj, uint64_t seed, uint32_t first_traj,
                    const Trunc& t, int save_every, int nobs, const int* obs_sites,
                    const double* obs_ops, double* obs_avg, int* njumps_per_traj, int max_jumps,
-                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats) {
+                   int* jumps, double* jumptimes, int blocks_per_sm, double* stats,
+                   bool classical) {
     Ctx* ctx = psi0->ctx;
     const int N = psi0->N, d = psi0->d;
     TN_REQUIRE(g->N == N && g->d == d, "GateList and MPS do not match.");
@@ -1284,6 +1300,7 @@ void qjmc_ensemble(const tn_mps* psi0, const tn_gates* g, int njump, const int* 
     p.njump = njump;
     p.maxj = maxj;
     p.nrows_out = nrows_out;
+    p.classical = classical ? 1 : 0;
     p.dt = dt;
     p.cutoff = t.cutoff;
     p.maxdim = (int)t.maxdim;

@@ -100,7 +100,7 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
                     const double* jops, const double* jcoeffs, int nsteps, double dt,
                     const double* draws, int64_t ndraws, const Trunc& t, int save_every,
                     int nobs, const int* obs_sites, const double* obs_ops, double* obs_out,
-                    int max_jumps) {
+                    int max_jumps, bool classical) {
     Ctx* ctx = psi->ctx;
     const int d = psi->d, N = psi->N;
     TN_REQUIRE(save_every >= 1, "save_every must be >= 1");
@@ -140,9 +140,44 @@ QjmcResult qjmc_run(tn_mps* psi, const tn_gates* g, int njump, const int* jsites
     };
     double time = 0.0;
     measure();
+    auto jump = [&](int idx) {
+        movecenter(psi, 1, no_trunc());
+        apply_site_op(psi, sites[idx], Lop[idx].c());
+        movecenter(psi, N, no_trunc());
+        movecenter(psi, 1, t);
+        mps_normalize(psi);
+        TN_REQUIRE((int)res.jumps.size() < max_jumps, "jump record capacity exceeded");
+    };
+    auto pick = [&](const std::vector<double>& rates, double er, double r) {
+        double cum = 0.0;
+        for (int j = 0; j < njump; ++j) {
+            cum += rates[j];
+            if (r < cum / er) return j;
+        }
+        return -1;
+    };
     for (int i = 1; i <= nsteps; ++i) {
         applygates(psi, g, t);
-        (void)draw();  // qjmc.jl:64 draws once per step; unused when classical
+        const double r0 = draw();  // qjmc.jl:64; the decision when not classical
+        if (!classical) {
+            // qjmc.jl:65-86: the jump probability is the norm lost in the step
+            const cplx n = mps_norm(psi);
+            const double prob = n.x * n.x;
+            mps_normalize(psi);
+            if (r0 > prob) {
+                std::vector<double> rates = qjmc_rates(psi, LdL, sites, coeffs);
+                double er = 0.0;
+                for (double r : rates) er += r;
+                const int idx = pick(rates, er, draw());
+                TN_REQUIRE(idx >= 0, "no jump channel selected (all rates zero)");
+                jump(idx);
+                res.jumps.push_back(idx + 1);
+                res.times.push_back(time + dt);
+            }
+            time += dt;
+            if (i % save_every == 0) measure();
+            continue;
+        }
         mps_normalize(psi);
         std::vector<double> rates = qjmc_rates(psi, LdL, sites, coeffs);
         double er = 0.0;

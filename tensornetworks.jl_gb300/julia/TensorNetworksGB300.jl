@@ -387,7 +387,8 @@ end
 # ---- qjmc_simulation (qjmc.jl:28-166), one trajectory, explicit draws --------
 function qjmc_simulation(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, tmax::Real, dt::Real,
                          observers=[]; save::Real=0, cutoff::Real=1e-12, mindim::Int=1, maxdim::Int=0,
-                         draws::Vector{Float64}=rand(3 * (ceil(Int, tmax / dt) + 1)), kwargs...)
+                         draws::Vector{Float64}=rand(3 * (ceil(Int, tmax / dt) + 1)),
+                         classical::Bool=true, kwargs...)
     save = save == 0 ? dt : save
     steps = Int(ceil(round(tmax / dt, digits=5)))
     savesteps = Int(ceil(round(save / dt)))
@@ -409,9 +410,10 @@ function qjmc_simulation(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, t
         check(ctx, ccall((:tn_qjmc_run, libtngpu), Int32,
                          (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{ComplexF64}, Ptr{ComplexF64},
                           Int32, Float64, Ptr{Float64}, Int64, Ref{TruncOpts}, Int32, Int32, Ptr{Int32},
-                          Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Int32}, Ptr{Float64}, Ref{Int32}, Ref{Int64}),
+                          Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Int32}, Ptr{Float64}, Ref{Int32}, Ref{Int64}, Int32),
                          ctx.h, hpsi, hg, length(jsites), jsites, jops, jco, steps, dt, draws, length(draws),
-                         t, savesteps, 0, C_NULL, C_NULL, C_NULL, jumps, jtimes, nj, used))
+                         t, savesteps, 0, C_NULL, C_NULL, C_NULL, jumps, jtimes, nj, used,
+                         Int32(classical)))
         download!(ctx, psi, hpsi)
     finally
         destroy_mps(hpsi)
@@ -448,11 +450,11 @@ function qjmc_ensemble(st::Sitetypes, psi::GMPS, H::OpList, jumpops::OpList, tma
                          (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Ptr{Int32}, Ptr{ComplexF64},
                           Ptr{ComplexF64}, Int32, Float64, Int32, Ptr{Float64}, Int64, UInt64, UInt32,
                           Ref{TruncOpts}, Int32, Int32, Ptr{Int32}, Ptr{ComplexF64}, Ptr{ComplexF64},
-                          Ptr{Int32}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}),
+                          Ptr{Int32}, Int32, Ptr{Int32}, Ptr{Float64}, Int32, Ptr{Float64}, Int32),
                          ctx.h, hpsi, hg, length(jsites), jsites, jops, jco, steps, dt, ntraj,
                          C_NULL, 0, UInt64(seed), UInt32(first_traj),
                          TruncOpts(cutoff, maxdim, mindim), savesteps, length(osites), osites,
-                         oops, avg, nj, 0, C_NULL, C_NULL, blocks_per_sm, C_NULL))
+                         oops, avg, nj, 0, C_NULL, C_NULL, blocks_per_sm, C_NULL, Int32(1)))
     finally
         destroy_mps(hpsi)
         ccall((:tn_gates_destroy, libtngpu), Int32, (Ptr{Cvoid},), hg)

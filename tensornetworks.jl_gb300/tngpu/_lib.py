@@ -89,12 +89,12 @@ _SIGS = {
                            C.c_double, dp, dp]),
     "tn_qjmc_rates": (i32, [P, P, i32, i32p, dp, dp, dp]),
     "tn_qjmc_run": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, dp, i64, C.POINTER(TruncOpts),
-                          i32, i32, i32p, dp, dp, i32p, dp, i32p, i64p]),
+                          i32, i32, i32p, dp, dp, i32p, dp, i32p, i64p, i32]),
     "tn_qjmc_batch": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, i32, dp, i64, C.c_uint64,
                             C.POINTER(TruncOpts), i32, i32, i32p, dp, dp, i32p, i32]),
     "tn_qjmc_ensemble": (i32, [P, P, P, i32, i32p, dp, dp, i32, f64, i32, dp, i64, C.c_uint64,
                                C.c_uint32, C.POINTER(TruncOpts), i32, i32, i32p, dp, dp, i32p,
-                               i32, i32p, dp, i32, dp]),
+                               i32, i32p, dp, i32, dp, i32]),
     "tn_philox_uniforms": (i32, [C.c_uint64, C.c_uint32, i64, dp]),
     "tn_heff2_apply": (i32, [P, i64, i64, i32, i64, i64, i64, dp, dp, dp, dp, dp, dp, i32]),
     "tn_heff2_apply_noalloc": (i32, [P, i64, i64, i32, i64, i64, i64, P, P, P, P, P, P]),

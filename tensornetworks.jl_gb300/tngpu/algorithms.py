@@ -398,7 +398,7 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
                   draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
                   seed=None, first_traj=0, engine="auto", blocks_per_sm=4, records=False,
-                  stats=None):
+                  stats=None, classical=True):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,
     averaged single-site observables [rows x terms], jump counts), and with
@@ -415,7 +415,8 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     trajectory at a time on its own stream (tn_qjmc_batch); "auto" takes the
     device engine whenever it applies.  ``stats`` (a dict) receives the
     device engine's algorithmic FP64 flops, launch time (CUDA events) and
-    trajectory-steps."""
+    trajectory-steps.  ``classical=False`` selects the norm-based jump
+    decision (qjmc.jl:65-86; device engine)."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -465,13 +466,15 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
             L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, int(first_traj),
             C.byref(t), savesteps, len(osites), osites.ctypes.data_as(L.i32p), L.as_dp(oops),
             L.as_dp(out), nj.ctypes.data_as(L.i32p), mj, jch.ctypes.data_as(L.i32p),
-            L.as_dp(jtm), int(blocks_per_sm), L.as_dp(sb)))
+            L.as_dp(jtm), int(blocks_per_sm), L.as_dp(sb), 1 if classical else 0))
         if stats is not None:
             stats.update(flops=float(sb[0]), kernel_ms=float(sb[1]), traj_steps=float(sb[2]),
                          blocks=int(sb[3]))
     else:
         if records:
             raise ValueError("jump records come from the device engine")
+        if not classical:
+            raise ValueError("the worker engine runs the escape-rate unraveling only")
         ctx.check(ctx.lib.tn_qjmc_batch(
             ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
             L.as_dp(jco), steps, float(dt), ntraj, dptr, ndraws, sd, C.byref(t), savesteps,
@@ -613,11 +616,11 @@ def qjmc_simulation(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, observe
     jumptimes) with 1-based jump indices.
 
     Uniform draws come from ``draws`` (an explicit array consumed in the
-    reference's order) or ``rand`` (a numpy Generator).  Single-site jump
-    operators and single-site observables run the whole trajectory inside the
-    library; other observers are sampled from the host between steps."""
-    if not classical:
-        raise NotImplementedError("the norm-based (classical=false) branch is not on this path")
+    reference's order) or ``rand`` (a numpy Generator).  ``classical=False``
+    decides jumps from the norm of the unnormalised state (qjmc.jl:65-86).
+    Single-site jump operators and single-site observables run the whole
+    trajectory inside the library; other observers are sampled from the host
+    between steps."""
     save = dt if save == 0 else save
     steps = math.ceil(round(tmax / dt, 5))
     savesteps = math.ceil(round(save / dt))
@@ -658,7 +661,8 @@ def qjmc_simulation(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, observe
             ctx.h, psi._h, gates._h, len(jsites), jsites.ctypes.data_as(L.i32p), L.as_dp(jops),
             L.as_dp(jco), steps, float(dt), L.as_dp(draws), draws.size, C.byref(t), savesteps,
             nobs, osites.ctypes.data_as(L.i32p), L.as_dp(oops), L.as_dp(out),
-            jumps.ctypes.data_as(L.i32p), L.as_dp(jtimes), C.byref(nj), C.byref(used)))
+            jumps.ctypes.data_as(L.i32p), L.as_dp(jtimes), C.byref(nj), C.byref(used),
+            1 if classical else 0))
         times = [0.0] + [dt * savesteps * (r + 1) for r in range(nrows - 1)]
         # reproduce the reference's accumulated time values
         tt, acc = 0.0, [0.0]
@@ -692,12 +696,13 @@ def qjmc_simulation(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, observe
     N = len(psi)
     for i in range(1, steps + 1):
         applygates(psi, gates, cutoff, maxdim, mindim)
-        nxt()
+        r0 = nxt()
+        prob = abs(psi.norm()) ** 2
         psi.normalize()
         ctx.check(ctx.lib.tn_qjmc_rates(ctx.h, psi._h, len(jsites), jsites.ctypes.data_as(L.i32p),
                                         L.as_dp(jops), L.as_dp(jco), L.as_dp(rates)))
         er = float(np.sum(rates))
-        if nxt() > math.exp(-er * dt):
+        if (r0 > prob) if not classical else (nxt() > math.exp(-er * dt)):
             r = nxt()
             idx = int(np.nonzero(r < np.cumsum(rates) / er)[0][0])
             psi.movecenter(1)

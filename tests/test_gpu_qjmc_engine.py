@@ -135,3 +135,33 @@ def test_engine_wide_bonds_match_oracle(tn):
                                          records=True)
     assert [list(map(int, j)) for j in jg] == jumps
     assert np.allclose(np.real(out), avg, atol=1e-9)
+
+
+def test_norm_based_unraveling_matches_oracle(tn):
+    """classical=false (qjmc.jl:65-86): the jump decision compares the
+    step's first draw with the squared norm of the unnormalised state.  The
+    single-trajectory driver and the engine both give the oracle's jump
+    records on the same streams."""
+    N, dt, steps, ntraj = 6, 0.05, 30, 6
+    draws = np.random.default_rng(77).random((ntraj, 3 * steps + 3))
+    Ho, Lo, _ = _model(O, N)
+    ref = []
+    for t in range(ntraj):
+        po = O.product_mps(O.spinhalf(), ["up"] * N)
+        j, jt = O.qjmc_simulation(O.spinhalf(), po, Ho, Lo, steps * dt, dt,
+                                  O.algorithms.UniformStream(draws[t]), cutoff=1e-10, maxdim=16,
+                                  classical=False)
+        ref.append((list(j), list(jt)))
+    assert sum(len(j) for j, _ in ref) > ntraj
+    Hg, Lg, Zg = _model(tn, N)
+    st = tn.spinhalf()
+    for t in range(2):
+        pg = tn.productMPS(st, ["up"] * N)
+        j, jt = tn.qjmc_simulation(st, pg, Hg, Lg, steps * dt, dt, cutoff=1e-10, maxdim=16,
+                                   classical=False, draws=draws[t])
+        assert j == ref[t][0] and np.allclose(jt, ref[t][1], rtol=0, atol=1e-12)
+    pg = tn.productMPS(st, ["up"] * N)
+    _, _, _, jg, jtg = tn.qjmc_ensemble(st, pg, Hg, Lg, steps * dt, dt, Zg, ntraj, draws=draws,
+                                        cutoff=1e-10, maxdim=16, engine="device", records=True,
+                                        classical=False)
+    assert [list(map(int, j)) for j in jg] == [j for j, _ in ref]

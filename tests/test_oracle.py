@@ -195,7 +195,11 @@ def test_qjmc_single_site_decay_closed_form():
     assert np.allclose(np.abs(psi[1].ravel()), [0, 1])
 
 
-def test_qjmc_matches_lindblad():
+@pytest.mark.parametrize("classical", [True, False])
+def test_qjmc_matches_lindblad(classical):
+    """Both unravelings of qjmc_simulation (classical=true: escape rates;
+    classical=false: the norm of the unnormalised state, qjmc.jl:65-86)
+    reproduce the Lindblad master equation statistically."""
     st = O.spinhalf()
     N, dt, T = 2, 0.02, 0.6
     H = O.OpList(N)
@@ -215,7 +219,7 @@ def test_qjmc_matches_lindblad():
         psi = O.product_mps(st, ["up", "up"])
         rec = {}
         O.qjmc_simulation(st, psi, H, L, T, dt, lambda: float(rng.random()), [zops],
-                          save=T, cutoff=1e-12, record=rec)
+                          save=T, cutoff=1e-12, record=rec, classical=classical)
         zs.append(np.real(rec["ops"][-1][0]))
     zs = np.array(zs)
     Hd = X.oplist_to_dense(st, H)
