@@ -75,6 +75,13 @@ typedef struct tn_dmrg_opts {
                                  optimisations (a bounded timing sample)  */
     int32_t profile_from_sweep; /* >= 0: enable the kernel profiler (see
                                    tn_profile_read) from this sweep index on */
+    int32_t refine;        /* mixed modes only, default 0: after each bond's
+                              Lanczos, `refine` refinement steps of the Ritz
+                              vector against its FP64 residual, each one
+                              Lanczos cycle (krylovdim products) whose first
+                              product is FP64 and fixes the projected
+                              matrix's first row; no reference counterpart
+                              (the reference's eigsolve is FP64 throughout) */
 } tn_dmrg_opts;
 
 typedef struct tn_dmrg_stats {
@@ -95,6 +102,12 @@ typedef struct tn_dmrg_stats {
     int32_t bond_cap;      /* optional per-bond records, capacity bond_cap */
     double* bond_seconds;  /* host wall seconds of each bond optimisation */
     int32_t* bond_chi;     /* max(chi_l, chi_r) of each optimised bond */
+    /* optional, capacity bond_cap: the FP64 residual ||H x - <x|H|x> x|| of
+     * each bond's unit eigenvector x before the refinement steps (the
+     * Lanczos output) and after them (the vector that is split); each costs
+     * one FP64 product unless a refinement step already made it */
+    double* bond_resid_in;
+    double* bond_resid_out;
 } tn_dmrg_stats;
 
 /* ---- kernel profiler ---------------------------------------------------------

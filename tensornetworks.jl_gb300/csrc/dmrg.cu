@@ -73,14 +73,24 @@ static void jacobi_eig(std::vector<double> A, int n, std::vector<double>& D, std
 struct LanczosOut {
     double eig;
     int64_t numops;
+    double resid0;  // ||(H - <x0|H|x0>) x0|| of the normalised start vector
 };
 
 using MatVec = std::function<void(const cplx*, cplx*)>;
 
+// With `first` given (one cycle, no restart): the start vector's product
+// comes from `first` and fixes the whole first row of the projected matrix,
+// (theta, rho, 0, ...) with theta the Rayleigh quotient and rho the residual
+// norm of that product; the later products come from `mv`, whose error then
+// enters only through the coefficients of the correction directions, which
+// are O(rho).  With an FP64 `first` and a tensor-core `mv` this is one
+// iterative-refinement step of the Ritz vector against its FP64 residual.
 static LanczosOut lanczos_lowest(Ctx* ctx, int64_t n, const cplx* x0, const MatVec& mv,
-                                 int krylovdim, int maxiter, double tol, DBuf& vec_out) {
+                                 int krylovdim, int maxiter, double tol, DBuf& vec_out,
+                                 const MatVec* first = nullptr) {
     TN_REQUIRE(krylovdim >= 1 && krylovdim <= 48, "krylovdim must be in 1..48");
     TN_REQUIRE(maxiter >= 1, "kryloviter must be >= 1");
+    TN_REQUIRE(!first || maxiter == 1, "a pinned first product allows one cycle only");
     const int kd = krylovdim;
     std::vector<DBuf> V(kd + 1);
     DBuf W(ctx, sizeof(cplx) * n);
@@ -95,10 +105,13 @@ static LanczosOut lanczos_lowest(Ctx* ctx, int64_t n, const cplx* x0, const MatV
     int K = 0, numiter = 1;
     int64_t numops = 0;
     std::vector<double> D, U;
-    double beta = 0;
+    double beta = 0, resid0 = 0;
     std::vector<const cplx*> ptr;
     for (;;) {
-        mv(V[K].c(), W.c());
+        if (first && K == 0)
+            (*first)(V[0].c(), W.c());
+        else
+            mv(V[K].c(), W.c());
         ++numops;
         ptr.clear();
         for (int j = 0; j <= K; ++j) ptr.push_back(V[j].c());
@@ -116,8 +129,13 @@ static LanczosOut lanczos_lowest(Ctx* ctx, int64_t n, const cplx* x0, const MatV
             h(j, K) = v;
             h(K, j) = v;
         }
+        if (first && K >= 1) {  // <x0|H v_K> = <H x0|v_K>: rho for K = 1, else 0
+            h(0, K) = K == 1 ? resid0 : 0.0;
+            h(K, 0) = h(0, K);
+        }
         ++K;
         beta = std::sqrt(znorm2(ctx, W.c(), n));
+        if (K == 1) resid0 = beta;
         const bool invariant = beta <= tol || K >= n;
         if (K < kd && !invariant) {
             zscale(ctx, W.c(), n, cmk(1.0 / beta, 0.0));
@@ -183,7 +201,17 @@ static LanczosOut lanczos_lowest(Ctx* ctx, int64_t n, const cplx* x0, const MatV
     zfill(ctx, vec_out.c(), n, cmk(0, 0));
     multi_axpy(ctx, vec_out.c(), ptr.data(), dU, K, n, 1.0);
     ctx->sync();
-    return LanczosOut{D[0], numops};
+    return LanczosOut{D[0], numops, resid0};
+}
+
+// ||H x - <x|H|x> x|| for a unit vector x, with the product from mv
+static double residual_norm(Ctx* ctx, int64_t n, const cplx* x, const MatVec& mv, DBuf& y) {
+    if (y.bytes < sizeof(cplx) * n) y = DBuf(ctx, sizeof(cplx) * n);
+    mv(x, y.c());
+    cplx* d = ctx->s_coef.c(ctx, 4);
+    multi_dot(ctx, &x, 1, y.c(), n, d);
+    multi_axpy(ctx, y.c(), &x, d, 1, n, -1.0);
+    return std::sqrt(znorm2(ctx, y.c(), n));
 }
 
 // ---- environment cache of <psi|H|psi> (ProjMPS, projmps.jl:16-95) ------------
@@ -292,6 +320,9 @@ void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double
                    o.precision == TN_PREC_MIXED_ENV64,
                "unknown precision");
     const bool mixed_heff = o.precision != TN_PREC_FP64;
+    TN_REQUIRE(o.refine >= 0 && o.refine <= 16, "refine must be in 0..16");
+    TN_REQUIRE(o.refine == 0 || mixed_heff,
+               "refine applies to the mixed precision modes (FP64 runs the reference's Lanczos)");
     auto t0 = std::chrono::steady_clock::now();
     // mixed precision: environment updates and truncation projections run on
     // the tensor cores for the whole call; restored on every exit path
@@ -333,7 +364,7 @@ void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double
     int64_t matvecs = 0;
     double last_disc = 0.0;
     const Trunc tr{o.cutoff, o.maxdim, o.mindim};
-    DBuf theta, vec, out, tmp;
+    DBuf theta, vec, out, tmp, tmp2;
     std::vector<MixedWork> mws(nh);
     std::vector<DBuf> kets(np), kets_c(np);
     int bond_updates = 0;
@@ -395,12 +426,13 @@ void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double
             }
             if (nh > 1 && tmp.bytes < sizeof(cplx) * n) tmp = DBuf(ctx, sizeof(cplx) * n);
             cplx* dproj = ctx->s_mixf.c(ctx, std::max<size_t>(np, 1));
-            // y = sum_t c_t H_t x + sum_p c_p K_p <K_p|x>  (product, projmpssum.jl:74-86)
-            MatVec mv = [&, cl, cr, site1](const cplx* x, cplx* y) {
+            // y = sum_t c_t H_t x + sum_p c_p K_p <K_p|x>  (product, projmpssum.jl:74-86);
+            // tensor cores for the MPO terms when tc (the mixed modes)
+            auto product = [&, cl, cr, site1](const cplx* x, cplx* y, bool tc) {
                 for (size_t t = 0; t < nh; ++t) {
                     cplx* dst = (t == 0) ? y : tmp.c();
                     const cplx* W12 = terms.H[t]->W12[site1 - 1].c();
-                    if (mixed_heff)
+                    if (tc)
                         mixed_heff2(ctx, mws[t], W12, cl, cr, d, lws[t], rws[t], x, dst);
                     else
                         heff2_fp64(ctx, Ls[t], W12, Rs[t], cl, cr, d, lws[t], rws[t], x, dst);
@@ -418,9 +450,28 @@ void dmrg_run(tn_mps* psi, const DmrgTerms& terms, const tn_dmrg_opts& o, double
                     multi_axpy(ctx, y, &kc, dproj + p, 1, n, 1.0);
                 }
             };
+            MatVec mv = [&](const cplx* x, cplx* y) { product(x, y, mixed_heff); };
+            MatVec mv64 = [&](const cplx* x, cplx* y) { product(x, y, false); };
             phase(1);
             LanczosOut lo = lanczos_lowest(ctx, n, theta.c(), mv, o.krylovdim, o.kryloviter, 1e-14, vec);
             matvecs += lo.numops;
+            // FP64-residual refinement of the Ritz vector (mixed modes): each
+            // step is one Lanczos cycle whose first product is FP64
+            const bool rec = stats && bond_updates < stats->bond_cap;
+            double rin = -1.0;
+            for (int s = 0; s < o.refine; ++s) {
+                LanczosOut lr = lanczos_lowest(ctx, n, vec.c(), mv, o.krylovdim, 1, 1e-14, vec, &mv64);
+                matvecs += lr.numops;
+                if (s == 0) rin = lr.resid0;
+                lo.eig = lr.eig;
+            }
+            if (rec && stats->bond_resid_in) {
+                if (rin < 0.0) rin = residual_norm(ctx, n, vec.c(), mv64, tmp2);
+                stats->bond_resid_in[bond_updates] = rin;
+            }
+            if (rec && stats->bond_resid_out)
+                stats->bond_resid_out[bond_updates] =
+                    (o.refine == 0 && rin >= 0.0) ? rin : residual_norm(ctx, n, vec.c(), mv64, tmp2);
             if (mixed_heff) tc_check_error(ctx);
             phase(2);
             cost = cmk(lo.eig, 0.0);

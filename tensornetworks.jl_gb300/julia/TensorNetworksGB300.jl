@@ -46,6 +46,7 @@ struct DmrgOpts
     verbose::Int32
     max_bond_updates::Int32
     profile_from_sweep::Int32
+    refine::Int32
 end
 
 mutable struct DmrgStats
@@ -63,8 +64,11 @@ mutable struct DmrgStats
     bond_cap::Int32
     bond_seconds::Ptr{Float64}
     bond_chi::Ptr{Int32}
+    bond_resid_in::Ptr{Float64}
+    bond_resid_out::Ptr{Float64}
 end
-DmrgStats() = DmrgStats(0, 0, 0, 0.0, 0.0, 0.0, 0, C_NULL, C_NULL, C_NULL, 0, 0, C_NULL, C_NULL)
+DmrgStats() = DmrgStats(0, 0, 0, 0.0, 0.0, 0.0, 0, C_NULL, C_NULL, C_NULL, 0, 0, C_NULL, C_NULL,
+                        C_NULL, C_NULL)
 
 mutable struct Context
     h::Ptr{Cvoid}
@@ -143,7 +147,7 @@ end
 function dmrg(psi::GMPS, H::GMPS; nsites::Int=2, krylovdim::Int=3, kryloviter::Int=2,
               minsweeps::Int=1, maxsweeps::Int=1000, tol::Float64=1e-10, tolgrad::Float64=1e-5,
               numconverges::Real=4, cutoff::Float64=1e-12, maxdim::Int=1000, mindim::Int=1,
-              verbose::Bool=true, precision::Symbol=:fp64, kwargs...)
+              verbose::Bool=true, precision::Symbol=:fp64, refine::Int=0, kwargs...)
     rank(psi) != 1 && error("Psi must be a GMPS of rank 1 (vector).")
     (length(H) != length(psi) || dim(H) != dim(psi)) && error("GMPS must share the same properties.")
     ctx = context()
@@ -151,7 +155,7 @@ function dmrg(psi::GMPS, H::GMPS; nsites::Int=2, krylovdim::Int=3, kryloviter::I
     hH = upload_mpo(ctx, H)
     opts = DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
                     Float64(numconverges), cutoff, maxdim, mindim,
-                    prec_code(precision), verbose, 0, -1)
+                    prec_code(precision), verbose, 0, -1, refine)
     energy = Ref{Float64}(0.0)
     stats = Ref(DmrgStats())
     try
@@ -173,10 +177,10 @@ function dmrg(psi::GMPS, Hs::GMPS...; coeffs=ones(length(Hs)), nsites::Int=2,
               krylovdim::Int=3, kryloviter::Int=2, minsweeps::Int=1, maxsweeps::Int=1000,
               tol::Float64=1e-10, tolgrad::Float64=1e-5, numconverges::Real=4,
               cutoff::Float64=1e-12, maxdim::Int=1000, mindim::Int=1, verbose::Bool=true,
-              precision::Symbol=:fp64, kwargs...)
+              precision::Symbol=:fp64, refine::Int=0, kwargs...)
     length(Hs) == 1 && rank(Hs[1]) == 2 && coeffs == [1] &&
         return dmrg(psi, Hs[1]; nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol,
-                    tolgrad, numconverges, cutoff, maxdim, mindim, verbose, precision)
+                    tolgrad, numconverges, cutoff, maxdim, mindim, verbose, precision, refine)
     ctx = context()
     hpsi = upload(ctx, psi)
     mpos = Ptr{Cvoid}[]; mc = Float64[]; projs = Ptr{Cvoid}[]; pc = Float64[]
@@ -190,7 +194,7 @@ function dmrg(psi::GMPS, Hs::GMPS...; coeffs=ones(length(Hs)), nsites::Int=2,
         end
         opts = DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
                         Float64(numconverges), cutoff, maxdim, mindim, prec_code(precision),
-                        verbose, 0, -1)
+                        verbose, 0, -1, refine)
         energy = Ref{Float64}(0.0)
         stats = Ref(DmrgStats())
         check(ctx, ccall((:tn_dmrg_sum, libtngpu), Int32,

@@ -8,8 +8,10 @@ observers, and the MPO algebra (``productMPO``, ``applyMPO``, ``adjoint``,
 ``libtngpu.so`` on the GPU; nothing here computes on the CPU beyond building
 model inputs (operator tables, MPO tensors, 4x4 gate exponentials and their
 output-index lifts) and re-laying out MPO sites for ``adjoint``.
+``tngpu.autotune`` holds the trajectory engine's launch-width autotuner.
 """
 
+from . import autotune  # noqa: F401
 from ._lib import Context, TNError, context, load  # noqa: F401
 from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEBDEnergy,  # noqa: F401
                          TEBDGradProblem, TEBDNorm, TEBDOperators, applygates, dmrg, qjmc_gates,

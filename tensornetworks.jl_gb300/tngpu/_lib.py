@@ -35,7 +35,8 @@ class DmrgOpts(C.Structure):
     _fields_ = [("nsites", i32), ("krylovdim", i32), ("kryloviter", i32), ("minsweeps", i32),
                 ("maxsweeps", i32), ("tol", f64), ("tolgrad", f64), ("numconverges", f64),
                 ("cutoff", f64), ("maxdim", i64), ("mindim", i64), ("precision", i32),
-                ("verbose", i32), ("max_bond_updates", i32), ("profile_from_sweep", i32)]
+                ("verbose", i32), ("max_bond_updates", i32), ("profile_from_sweep", i32),
+                ("refine", i32)]
 
 
 class VmpsOpts(C.Structure):
@@ -48,7 +49,8 @@ class DmrgStats(C.Structure):
     _fields_ = [("sweeps", i32), ("maxbonddim", i32), ("matvecs", i64), ("seconds", f64),
                 ("energy_fp64", f64), ("last_discarded", f64), ("sweep_cap", i32),
                 ("sweep_seconds", dp), ("sweep_energies", dp), ("sweep_maxdim", i32p),
-                ("bond_updates", i32), ("bond_cap", i32), ("bond_seconds", dp), ("bond_chi", i32p)]
+                ("bond_updates", i32), ("bond_cap", i32), ("bond_seconds", dp), ("bond_chi", i32p),
+                ("bond_resid_in", dp), ("bond_resid_out", dp)]
 
 
 _SIGS = {

@@ -24,7 +24,7 @@ from .mps import GMPS, MPOHandle, MPSProjector, applyMPO, inner
 def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
          maxsweeps=1000, tol=1e-10, tolgrad=1e-5, numconverges=4, cutoff=1e-12, maxdim=1000,
          mindim=1, verbose=True, precision="fp64", stats=None, max_bond_updates=0,
-         profile_from_sweep=-1, coeffs=None):
+         profile_from_sweep=-1, coeffs=None, refine=0, residuals=False):
     """Two-site DMRG; mutates ``psi`` and returns (psi, energy).
 
     ``Hs`` are the terms of dmrg(psi, Hs::GMPS...; coeffs) (dmrg.jl:128-154):
@@ -32,9 +32,15 @@ def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
     ProjMPS(phi, psi; squared=true) gives), weighted by ``coeffs`` (default
     all 1).  ``precision``: "fp64", "mixed" (3xTF32 tensor-core H_eff,
     environments and projections) or "mixed-env64" (the same with FP64
-    environment updates).  ``stats`` (a dict) receives sweeps, matvecs,
-    per-sweep device seconds and energies; ``max_bond_updates`` > 0 stops
-    after that many bond optimisations (a bounded timing sample)."""
+    environment updates).  ``refine`` (mixed modes): refinement steps of each
+    bond's Ritz vector against its FP64 residual, one Lanczos cycle each
+    whose first product is FP64.  ``stats`` (a dict) receives sweeps,
+    matvecs, per-sweep device seconds and energies, and with ``residuals``
+    the FP64 residual norm of every bond's eigenvector before and after the
+    refinement (``bond_resid_in``/``bond_resid_out``; one extra FP64 product
+    per bond and value that a refinement step did not already make);
+    ``max_bond_updates`` > 0 stops after that many bond optimisations (a
+    bounded timing sample)."""
     if psi.rank != 1:
         raise ValueError("Psi must be a GMPS of rank 1 (vector).")
     if len(Hs) == 0:
@@ -51,7 +57,7 @@ def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
         raise ValueError("only two-site DMRG (nsites=2) is on this path")
     o = L.DmrgOpts(nsites, krylovdim, kryloviter, minsweeps, maxsweeps, tol, tolgrad,
                    float(numconverges), cutoff, maxdim, mindim, L.PREC[precision], int(bool(verbose)),
-                   int(max_bond_updates), int(profile_from_sweep))
+                   int(max_bond_updates), int(profile_from_sweep), int(refine))
     e = C.c_double()
     st = L.DmrgStats()
     cap = maxsweeps if maxsweeps > 0 else 1000
@@ -65,6 +71,9 @@ def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
     bchi = np.zeros(bcap, dtype=np.int32)
     st.bond_cap = bcap
     st.bond_seconds, st.bond_chi = L.as_dp(bsec), bchi.ctypes.data_as(L.i32p)
+    rin, rout = np.zeros(bcap), np.zeros(bcap)
+    if residuals:
+        st.bond_resid_in, st.bond_resid_out = L.as_dp(rin), L.as_dp(rout)
     ctx = psi.ctx
     if len(Hs) == 1 and Hs[0].rank == 2 and coeffs[0] == 1.0:
         ctx.check(ctx.lib.tn_dmrg(ctx.h, psi._h, Hs[0]._h, C.byref(o), C.byref(e), C.byref(st)))
@@ -86,6 +95,9 @@ def dmrg(psi: GMPS, *Hs, nsites=2, krylovdim=3, kryloviter=2, minsweeps=1,
                      sweep_maxdim=mds[: min(st.sweeps, cap)].tolist(),
                      bond_seconds=bsec[: min(st.bond_updates, bcap)].tolist(),
                      bond_chi=bchi[: min(st.bond_updates, bcap)].tolist())
+        if residuals:
+            stats.update(bond_resid_in=rin[: min(st.bond_updates, bcap)].tolist(),
+                         bond_resid_out=rout[: min(st.bond_updates, bcap)].tolist())
     return psi, e.value
 
 
@@ -398,7 +410,7 @@ def qjmc_gates(st, H: OpList, jumpops: OpList, dt, **kw):
 def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpList, ntraj,
                   draws=None, rand=None, save=0.0, cutoff=1e-12, mindim=1, maxdim=0, workers=64,
                   seed=None, first_traj=0, engine="auto", blocks_per_sm=4, records=False,
-                  stats=None, classical=True):
+                  stats=None, classical=True, tune_cache=None, probe_steps=8):
     """``ntraj`` independent trajectories of qjmc_simulation from ``psi``
     (left unchanged), advanced concurrently on the GPU.  Returns (times,
     averaged single-site observables [rows x terms], jump counts), and with
@@ -411,6 +423,11 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     engine="device" runs the whole ensemble as one persistent launch
     (tn_qjmc_ensemble: every block runs whole trajectories, ``blocks_per_sm``
     blocks per SM; needs maxdim >= 1 with d * maxdim <= 256);
+    blocks_per_sm="auto" takes the width the autotuner picked for this
+    workload's (maxdim, d, ntraj, N) bucket (tngpu.autotune), probing the
+    first ``probe_steps`` steps of this ensemble at every candidate width on
+    a cache miss (``tune_cache``: a WidthCache or a JSON path; default
+    $TNGPU_TUNE_CACHE or ~/.cache/tngpu/engine_widths.json);
     engine="workers" runs ``workers`` host threads, each driving one
     trajectory at a time on its own stream (tn_qjmc_batch); "auto" takes the
     device engine whenever it applies.  ``stats`` (a dict) receives the
@@ -456,6 +473,23 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     nj = np.zeros(ntraj, dtype=np.int32)
     t = L.trunc(cutoff, maxdim, mindim)
     ctx = psi.ctx
+    if engine == "device" and blocks_per_sm == "auto":
+        from . import autotune as AT
+        cache = tune_cache if isinstance(tune_cache, AT.WidthCache) else AT.WidthCache(tune_cache)
+        pk = max(1, min(steps, int(probe_steps)))
+
+        def probe(w):
+            s = {}
+            qjmc_ensemble(st, psi, H, jumpops, pk * dt, dt, obs, ntraj, draws=draws, seed=seed,
+                          first_traj=first_traj, save=dt, cutoff=cutoff, mindim=mindim,
+                          maxdim=maxdim, engine="device", blocks_per_sm=w, stats=s,
+                          classical=classical)
+            return s["kernel_ms"] * 1e-3 / max(s["traj_steps"], 1.0)
+
+        key = AT.bucket(maxdim, st.dim, ntraj, H.length)
+        blocks_per_sm, timings = AT.tune(key, probe, cache=cache)
+        if stats is not None:
+            stats.update(tune_key=key, tune_seconds_per_traj_step=timings)
     if engine == "device":
         mj = steps + 1 if records else 0
         jch = np.zeros((ntraj, max(mj, 1)), dtype=np.int32)
@@ -469,7 +503,7 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
             L.as_dp(jtm), int(blocks_per_sm), L.as_dp(sb), 1 if classical else 0))
         if stats is not None:
             stats.update(flops=float(sb[0]), kernel_ms=float(sb[1]), traj_steps=float(sb[2]),
-                         blocks=int(sb[3]))
+                         blocks=int(sb[3]), blocks_per_sm=int(blocks_per_sm))
     else:
         if records:
             raise ValueError("jump records come from the device engine")

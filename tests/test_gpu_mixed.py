@@ -146,3 +146,47 @@ def test_tebd_mixed_matches_fp64(tn):
     assert dmx == d64
     assert np.max(np.abs(zmx - z64)) <= 1e-5, np.max(np.abs(zmx - z64))
     assert abs(smx - s64) <= 1e-5, (smx, s64)
+
+
+def test_dmrg_fp64_residual_refinement(tn):
+    """refine (mixed modes): each bond's Ritz vector gets refinement steps
+    against its FP64 residual, one Lanczos cycle each whose first product is
+    FP64 and fixes the projected matrix's first row.  From a state converged
+    by FP64 DMRG, one mixed-env64 sweep pair without and with two refinement
+    steps; the FP64 residual norms of the split vectors come back per bond.
+    Without refinement the residual reported after equals the one before
+    (the same vector); with it the median residual falls at least 3x and the
+    largest does not grow; both energies stay within 1e-9 of FP64.  FP64
+    mode rejects refine (its Lanczos is the reference's)."""
+    N, D = 16, 8
+    rng = np.random.default_rng(5)
+    shapes = [((1 if i == 0 else D), 2, (1 if i == N - 1 else D)) for i in range(N)]
+    draws = [O.fr(rng.standard_normal(int(np.prod(s))), s) for s in shapes]
+    draws.append(O.fr(rng.standard_normal(4), (1, 2, 2)))
+    po = O.random_mps(2, N, D, draws)
+    W = tn.MPO(tn.spinhalf(), _xxz(tn, N))
+    kw = dict(maxdim=64, cutoff=1e-12, numconverges=np.inf, verbose=False)
+    p = tn.GMPS.from_tensors(po.tensors, po.center)
+    st = {}
+    tn.dmrg(p, W, minsweeps=6, maxsweeps=6, stats=st, **kw)
+    E64 = st["energy_fp64"]
+    tensors, center = p.tensors(), p.center
+    res = {}
+    for r in (0, 2):
+        q = tn.GMPS.from_tensors(tensors, center)
+        s = {}
+        tn.dmrg(q, W, minsweeps=2, maxsweeps=2, precision="mixed-env64", refine=r, residuals=True,
+                stats=s, **kw)
+        res[r] = (np.array(s["bond_resid_in"]), np.array(s["bond_resid_out"]), s["energy_fp64"])
+        assert len(res[r][0]) == 2 * (N - 1) and np.all(res[r][0] > 0)
+        assert abs(s["energy_fp64"] - E64) <= 1e-9 * abs(E64), (r, s["energy_fp64"], E64)
+    rin0, rout0, _ = res[0]
+    rin, rout, _ = res[2]
+    print("refine=0 resid:", np.median(rin0), rin0.max())
+    print("refine=2 resid in/out:", np.median(rin), rin.max(), np.median(rout), rout.max())
+    assert np.array_equal(rin0, rout0)
+    assert np.median(rout) <= np.median(rin) / 3
+    assert rout.max() <= rin.max()
+    q = tn.GMPS.from_tensors(tensors, center)
+    with pytest.raises(tn.TNError, match="refine"):
+        tn.dmrg(q, W, minsweeps=1, maxsweeps=1, refine=1, **kw)

@@ -165,3 +165,31 @@ def test_norm_based_unraveling_matches_oracle(tn):
                                         cutoff=1e-10, maxdim=16, engine="device", records=True,
                                         classical=False)
     assert [list(map(int, j)) for j in jg] == [j for j, _ in ref]
+
+
+def test_engine_autotuned_width(tn, tmp_path):
+    """blocks_per_sm="auto": on a cache miss the autotuner times the first
+    steps of the ensemble at every width (the engine's CUDA-event launch
+    time per trajectory-step) and keeps the fastest for the workload's
+    bucket; the run gives the trajectories of any fixed width; a second call
+    takes the width from the cache without probing."""
+    N, dt, steps, ntraj = 8, 0.05, 20, 40
+    H, Lj, Z = _model(tn, N)
+    st = tn.spinhalf()
+    psi = tn.productMPS(st, ["up"] * N)
+    kw = dict(seed=3, cutoff=1e-10, maxdim=16, engine="device", records=True)
+    path = str(tmp_path / "widths.json")
+    s = {}
+    ra = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, blocks_per_sm="auto",
+                          tune_cache=path, stats=s, **kw)
+    timings = s["tune_seconds_per_traj_step"]
+    print("probe seconds per trajectory-step:", timings, "->", s["blocks_per_sm"])
+    assert s["tune_key"] == tn.autotune.bucket(16, 2, ntraj, N)
+    assert sorted(timings) == [1, 2, 4, 8] and all(t > 0 for t in timings.values())
+    assert s["blocks_per_sm"] == min(timings, key=lambda w: (timings[w], w))
+    rb = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, blocks_per_sm=1, **kw)
+    assert np.array_equal(ra[1], rb[1]) and ra[3] == rb[3] and ra[4] == rb[4]
+    s2 = {}
+    tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, blocks_per_sm="auto",
+                     tune_cache=path, stats=s2, **kw)
+    assert s2["tune_seconds_per_traj_step"] == {} and s2["blocks_per_sm"] == s["blocks_per_sm"]
