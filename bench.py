@@ -66,7 +66,9 @@ def parse():
     p.add_argument("--qjmc-steps", type=int, default=500, help="qjmc: steps per trajectory")
     p.add_argument("--qjmc-single", type=int, default=2,
                    help="qjmc: trajectories of the one-at-a-time arm")
-    p.add_argument("--blocks-per-sm", type=int, default=4, help="qjmc: engine blocks per SM")
+    p.add_argument("--blocks-per-sm", default="4",
+                   help="qjmc: engine blocks per SM (1, 2, 4, 8), or 'auto' for the autotuner's "
+                        "pick, tuned before the timed run")
     p.add_argument("--qjmc-pre", type=int, default=0,
                    help="qjmc: start every trajectory from one trajectory evolved this many "
                         "steps (untimed) instead of the all-up state")
@@ -679,11 +681,20 @@ def qjmc_run(args):
     fp64_peak = cublas_zgemm_tflops(ctx.device)
     # warm-up: a short ensemble (module load, pools)
     tn.qjmc_ensemble(st, psi, H, Lj, 2 * dt, dt, Z, 8, seed=seed, engine="device", **kw)
+    tune = None
+    if args.blocks_per_sm == "auto":
+        width, timings, key = tn.tune_qjmc_width(st, psi, H, Lj, dt, Z, ntraj, seed=seed, **kw)
+        tune = {"bucket": key, "width": width,
+                "probe_seconds_per_traj_step": {str(w): t for w, t in timings.items()},
+                "probe": "the first 8 steps of this ensemble at each width (empty: cached)"}
+        log(f"qjmc autotune: {tune}")
+    else:
+        width = int(args.blocks_per_sm)
     clk = Clocks(ctx.device)
     stt = {}
     t0 = time.perf_counter()
     times, zav, nj = tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, seed=seed,
-                                      engine="device", blocks_per_sm=args.blocks_per_sm,
+                                      engine="device", blocks_per_sm=width,
                                       stats=stt, **kw)
     wall = time.perf_counter() - t0
     clocks = clk.stop()
@@ -742,7 +753,7 @@ def qjmc_run(args):
                                    + (f"state of one trajectory after {args.qjmc_pre} steps "
                                       f"(chi {start_chi})" if args.qjmc_pre else "all-up"),
                        "engine": f"persistent launch, {stt['blocks']} blocks "
-                                 f"({args.blocks_per_sm} per SM)"},
+                                 f"({width} per SM)", "autotune": tune},
             "wall_traj_steps_per_s": rate, "wall_s": wall,
             "single_trajectory_traj_steps_per_s": single,
             "batched_vs_single": rate / single if single else None,

@@ -16,7 +16,7 @@ from ._lib import Context, TNError, context, load  # noqa: F401
 from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEBDEnergy,  # noqa: F401
                          TEBDGradProblem, TEBDNorm, TEBDOperators, applygates, dmrg, qjmc_gates,
                          philox_uniforms, qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation,
-                         shard_range, tebd,
+                         shard_range, tebd, tune_qjmc_width,
                          tebd_grad, trotterize, vmps)
 from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
 from .mps import (GMPO, GMPS, MPO, MPOHandle, MPSProjector, adjoint, applyMPO, as_gmpo,  # noqa: F401

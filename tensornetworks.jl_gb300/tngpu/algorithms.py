@@ -474,20 +474,10 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
     t = L.trunc(cutoff, maxdim, mindim)
     ctx = psi.ctx
     if engine == "device" and blocks_per_sm == "auto":
-        from . import autotune as AT
-        cache = tune_cache if isinstance(tune_cache, AT.WidthCache) else AT.WidthCache(tune_cache)
-        pk = max(1, min(steps, int(probe_steps)))
-
-        def probe(w):
-            s = {}
-            qjmc_ensemble(st, psi, H, jumpops, pk * dt, dt, obs, ntraj, draws=draws, seed=seed,
-                          first_traj=first_traj, save=dt, cutoff=cutoff, mindim=mindim,
-                          maxdim=maxdim, engine="device", blocks_per_sm=w, stats=s,
-                          classical=classical)
-            return s["kernel_ms"] * 1e-3 / max(s["traj_steps"], 1.0)
-
-        key = AT.bucket(maxdim, st.dim, ntraj, H.length)
-        blocks_per_sm, timings = AT.tune(key, probe, cache=cache)
+        blocks_per_sm, timings, key = tune_qjmc_width(
+            st, psi, H, jumpops, dt, obs, ntraj, probe_steps=min(steps, int(probe_steps)),
+            cache=tune_cache, draws=draws, seed=seed, first_traj=first_traj, cutoff=cutoff,
+            mindim=mindim, maxdim=maxdim, classical=classical)
         if stats is not None:
             stats.update(tune_key=key, tune_seconds_per_traj_step=timings)
     if engine == "device":
@@ -523,6 +513,32 @@ def qjmc_ensemble(st, psi: GMPS, H: OpList, jumpops: OpList, tmax, dt, obs: OpLi
         return (times, out, nj, [list(jch[r, :nj[r]]) for r in range(ntraj)],
                 [list(jtm[r, :nj[r]]) for r in range(ntraj)])
     return times, out, nj
+
+
+def tune_qjmc_width(st, psi, H, jumpops, dt, obs, ntraj, probe_steps=8, cache=None, **kw):
+    """The trajectory engine's launch width (blocks per SM) for this
+    ensemble, from the autotuner (tngpu.autotune): the cached width of the
+    workload's (maxdim, d, ntraj, N) bucket, or on a miss the fastest width
+    over the first ``probe_steps`` steps of this ensemble (``kw``: the
+    draws or seed and truncation of qjmc_ensemble), timed by the engine's
+    CUDA events per trajectory-step and then cached.  ``cache``: a
+    WidthCache or a JSON path (None: the default path).  Returns (width,
+    {width: seconds per trajectory-step} -- empty on a cache hit, key)."""
+    from . import autotune as AT
+    cache = cache if isinstance(cache, AT.WidthCache) else AT.WidthCache(cache)
+    pk = max(1, int(probe_steps))
+    kw = {k: v for k, v in kw.items()
+          if k not in ("save", "engine", "blocks_per_sm", "stats", "records")}
+
+    def probe(w):
+        s = {}
+        qjmc_ensemble(st, psi, H, jumpops, pk * dt, dt, obs, ntraj, save=dt, engine="device",
+                      blocks_per_sm=w, stats=s, **kw)
+        return s["kernel_ms"] * 1e-3 / max(s["traj_steps"], 1.0)
+
+    key = AT.bucket(kw.get("maxdim", 0), st.dim, ntraj, H.length)
+    width, timings = AT.tune(key, probe, cache=cache)
+    return width, timings, key
 
 
 def philox_uniforms(seed, trajectory, n):

@@ -193,3 +193,7 @@ def test_engine_autotuned_width(tn, tmp_path):
     tn.qjmc_ensemble(st, psi, H, Lj, steps * dt, dt, Z, ntraj, blocks_per_sm="auto",
                      tune_cache=path, stats=s2, **kw)
     assert s2["tune_seconds_per_traj_step"] == {} and s2["blocks_per_sm"] == s["blocks_per_sm"]
+    # the bench's form: the tuner on its own, with qjmc_ensemble's keywords
+    w, t, key = tn.tune_qjmc_width(st, psi, H, Lj, dt, Z, ntraj, cache=path, seed=3,
+                                   cutoff=1e-10, maxdim=16, save=10 * dt)
+    assert (w, t, key) == (s["blocks_per_sm"], {}, s["tune_key"])
