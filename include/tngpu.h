@@ -69,7 +69,7 @@ typedef struct tn_dmrg_opts {
     double cutoff;         /* default 1e-12                               */
     int64_t maxdim;        /* default 1000                                */
     int64_t mindim;        /* default 1                                   */
-    int32_t precision;     /* TN_PREC_FP64 or TN_PREC_MIXED               */
+    int32_t precision;     /* TN_PREC_FP64, _MIXED or _MIXED_ENV64        */
     int32_t verbose;       /* print the reference's per-sweep line        */
     int32_t max_bond_updates; /* 0 = run the sweeps; n > 0 = stop after n bond
                                  optimisations (a bounded timing sample)  */
