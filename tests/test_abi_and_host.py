@@ -203,3 +203,57 @@ def test_output_index_gate_lift():
     thf = np.reshape(th, (3, d * d, d * d, 4), order="F")
     got2 = np.einsum("PKQL,aKLb->aPQb", L2, thf)
     assert np.allclose(np.reshape(got2, (3, d, d, d, d, 4), order="F"), ref2)
+
+
+# C struct -> (ctypes mirror, Julia shim struct)
+_STRUCTS = {"tn_trunc_opts": ("TruncOpts", "TruncOpts"), "tn_dmrg_opts": ("DmrgOpts", "DmrgOpts"),
+            "tn_dmrg_stats": ("DmrgStats", "DmrgStats"), "tn_vmps_opts": ("VmpsOpts", "VmpsOpts")}
+_JL_SIZES = {"Int32": 4, "Int64": 8, "Float64": 8}
+
+
+def _header_struct_fields(name):
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), open(HEADER).read(), re.S)
+    body = re.sub(r"/\*.*?\*/", "", body.group(1), flags=re.S)
+    return re.findall(r"^\s*[\w\s\*]+?[\s\*](\w+)\s*;", body, re.M)
+
+
+def _julia_struct_fields(name):
+    src = open(os.path.join(ROOT, "tensornetworks.jl_gb300", "julia", "TensorNetworksGB300.jl")).read()
+    body = re.search(r"^(?:mutable )?struct %s\n(.*?)^end" % name, src, re.S | re.M).group(1)
+    return re.findall(r"^\s*(\w+)::(\w+(?:\{\w+\})?)", body, re.M)
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every option/stats struct of the header: gcc's sizeof and offsetof
+    equal the ctypes mirror's, and the Julia shim declares the same fields in
+    the same order with types of the same sizes (C layout rules then give
+    the same offsets)."""
+    from tngpu import _lib as L
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "tngpu.h"', "int main(void) {"]
+    fields = {s: _header_struct_fields(s) for s in _STRUCTS}
+    for s, fs in fields.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (s, s))
+        for f in fs:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (s, f, s, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n"):
+        if ln:
+            s, f, v = ln.split()
+            got[(s, f)] = int(v)
+    for s, (py, jl) in _STRUCTS.items():
+        cls = getattr(L, py)
+        assert [f for f, _ in cls._fields_] == fields[s], s
+        assert ctypes.sizeof(cls) == got[(s, "size")], s
+        for f in fields[s]:
+            assert getattr(cls, f).offset == got[(s, f)], (s, f)
+        jf = _julia_struct_fields(jl)
+        assert [f for f, _ in jf] == fields[s], (jl, jf)
+        for (f, t), (_, ct) in zip(jf, cls._fields_):
+            size = 8 if t.startswith("Ptr") else _JL_SIZES[t]
+            assert size == ctypes.sizeof(ct), (jl, f, t)
