@@ -257,3 +257,96 @@ def test_struct_layouts_match_header(tmp_path):
         for (f, t), (_, ct) in zip(jf, cls._fields_):
             size = 8 if t.startswith("Ptr") else _JL_SIZES[t]
             assert size == ctypes.sizeof(ct), (jl, f, t)
+
+
+def _split_top(s):
+    """Split s at commas outside (), {} and []."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def _balanced(s, i):
+    """The text inside the parenthesis opening at s[i]."""
+    depth = 0
+    for j in range(i, len(s)):
+        depth += s[j] == "("
+        depth -= s[j] == ")"
+        if depth == 0:
+            return s[i + 1:j]
+    raise ValueError("unbalanced")
+
+
+def _c_kind(param):
+    param = re.sub(r"/\*.*?\*/", "", param).strip()
+    if "*" in param:
+        return "ptr"
+    for t, k in (("uint64_t", "u64"), ("int64_t", "i64"), ("uint32_t", "u32"), ("int32_t", "i32"),
+                 ("double", "f64")):
+        if param.startswith(t) or param.startswith("const " + t):
+            return k
+    raise ValueError(param)
+
+
+def _jl_kind(t):
+    t = t.strip()
+    if t.startswith(("Ptr", "Ref", "Cstring")):
+        return "ptr"
+    return {"Int32": "i32", "Cint": "i32", "Int64": "i64", "UInt64": "u64", "UInt32": "u32",
+            "Float64": "f64"}[t]
+
+
+def _header_decls():
+    hdr = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    decl = {}
+    for m in re.finditer(r"^\s*(?:int32_t|int64_t|const char\*)\s+(tn_\w+)\s*\(", hdr, re.M):
+        params = _balanced(hdr, m.end() - 1)
+        ps = [] if params.strip() in ("", "void") else _split_top(params)
+        decl[m.group(1)] = [_c_kind(p) for p in ps]
+    return decl
+
+
+def test_python_signatures_match_header():
+    """Every ctypes signature of the Python binding has the header's
+    argument count and kinds."""
+    from tngpu import _lib
+    kinds = {ctypes.c_int32: "i32", ctypes.c_int64: "i64", ctypes.c_uint64: "u64",
+             ctypes.c_uint32: "u32", ctypes.c_double: "f64"}
+    decl = _header_decls()
+    for name, (_, args) in _lib._SIGS.items():
+        got = []
+        for a in args:
+            if a in kinds:
+                got.append(kinds[a])
+            else:
+                assert a in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(a, ctypes._Pointer), \
+                    (name, a)
+                got.append("ptr")
+        assert got == decl[name], (name, got, decl[name])
+
+
+def test_julia_shim_ccalls_match_header():
+    """Every ccall of the Julia shim names a header entry point and passes
+    the header's number of arguments, each of the same kind (pointer, int32,
+    int64, uint64, double) -- the static half of a binding check, since no
+    Julia runs here."""
+    decl = _header_decls()
+    src = open(os.path.join(ROOT, "tensornetworks.jl_gb300", "julia", "TensorNetworksGB300.jl")).read()
+    calls = list(re.finditer(r"ccall\(\(:(tn_\w+), libtngpu\),\s*[\w{}]+,\s*\(", src))
+    assert len(calls) >= 25
+    for m in calls:
+        name = m.group(1)
+        assert name in decl, name
+        kinds = [_jl_kind(t) for t in _split_top(_balanced(src, m.end() - 1))]
+        assert kinds == decl[name], (name, kinds, decl[name])
