@@ -195,6 +195,28 @@ def test_qjmc_single_site_decay_closed_form():
     assert np.allclose(np.abs(psi[1].ravel()), [0, 1])
 
 
+def test_qjmc_single_site_decay_closed_form_norm_based():
+    """classical=false (qjmc.jl:65-86), H = 0, L = sqrt(g) s-: from |up> the
+    unnormalised state after a step has squared norm exp(-g dt), so a jump
+    happens at the first step whose one draw exceeds it (a second draw then
+    picks the channel); after it |down> keeps norm 1 and never jumps again."""
+    st = O.spinhalf()
+    N, g, dt = 1, 0.3, 0.01
+    H = O.OpList(N)
+    H.add("z", 1, 0.0)
+    L = O.OpList(N)
+    L.add("s-", 1, np.sqrt(g))
+    p = np.exp(-g * dt)
+    # step 1 just below the threshold, step 2 just above it (then the pick),
+    # steps 3-4 at the top of [0, 1)
+    draws = [p - 1e-9, p + 1e-9, 0.7, 0.999999, 0.999999]
+    psi = O.product_mps(st, ["up"])
+    jumps, times = O.qjmc_simulation(st, psi, H, L, 4 * dt, dt, O.algorithms.UniformStream(draws),
+                                     cutoff=1e-12, classical=False)
+    assert jumps == [1] and abs(times[0] - 2 * dt) < 1e-15
+    assert np.allclose(np.abs(psi[1].ravel()), [0, 1])
+
+
 @pytest.mark.parametrize("classical", [True, False])
 def test_qjmc_matches_lindblad(classical):
     """Both unravelings of qjmc_simulation (classical=true: escape rates;
