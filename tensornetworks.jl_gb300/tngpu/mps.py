@@ -409,10 +409,11 @@ def movecenter(psi, idx, **kw):
 
 
 # ---------------------------------------------------------------------------
-# Checkpoints (the GMPS HDF5 group of gmps.jl:359-383, as an .npz archive:
-# h5py is not a dependency).  The group's fields keep their names and
-# meaning: attributes type="MPS" and version=1, datasets "length", "center"
-# and "MPS[i]" (1-based, [Dl, d, Dr] complex).
+# Checkpoints: the GMPS HDF5 group of gmps.jl:359-383 (attributes type="MPS"
+# and version=1, datasets "length", "center" and "MPS[i]", 1-based, the site
+# tensors complex [Dl, d, Dr] or [Dl, d, d, Dr]).  Paths ending in .h5 or
+# .hdf5 are HDF5 files in HDF5.jl's layout (tngpu.h5); other paths hold the
+# same group as entries of an .npz archive.
 # ---------------------------------------------------------------------------
 def mps_record(tensors, center, name="psi"):
     """The archive entries of one MPS group."""
@@ -432,13 +433,30 @@ def mps_from_record(rec, name="psi"):
     return [np.asarray(rec[f"{name}/MPS[{i}]"]) for i in range(1, N + 1)], int(rec[f"{name}/center"])
 
 
+def _is_hdf5(path):
+    return str(path).lower().endswith((".h5", ".hdf5"))
+
+
 def write_mps(path, psi, name="psi"):
-    """Download psi and store it as the group ``name`` of an .npz archive."""
-    np.savez(path, **mps_record(psi.tensors(), psi.center, name))
+    """Download psi (a GMPS or GMPO) and store it as the group ``name`` of
+    an HDF5 file (a .h5/.hdf5 path) or of an .npz archive."""
+    if _is_hdf5(path):
+        from . import h5
+        h5.write_gmps(path, psi.tensors(), psi.center, name)
+    else:
+        np.savez(path, **mps_record(psi.tensors(), psi.center, name))
 
 
 def read_mps(path, name="psi", ctx=None):
-    """Upload the MPS group ``name`` of an archive written by write_mps."""
-    with np.load(path, allow_pickle=False) as z:
-        tensors, center = mps_from_record({k: z[k] for k in z.files}, name)
+    """Upload the group ``name`` written by write_mps (or, for an HDF5
+    file, by the reference's HDF5.write): a GMPS, or a GMPO when the site
+    tensors have two physical indices (the rank test of gmps.jl:380-382)."""
+    if _is_hdf5(path):
+        from . import h5
+        tensors, center = h5.read_gmps(path, name)
+    else:
+        with np.load(path, allow_pickle=False) as z:
+            tensors, center = mps_from_record({k: z[k] for k in z.files}, name)
+    if np.ndim(tensors[0]) == 4:
+        return GMPO.from_tensors(tensors, center, ctx)
     return GMPS.from_tensors(tensors, center, ctx)

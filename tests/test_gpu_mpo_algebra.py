@@ -90,17 +90,18 @@ def test_thermal_state_matches_oracle_and_ed(tn):
     assert abs(E - np.sum(w * ev) / np.sum(w)) < 1e-4
 
 
-def test_mps_checkpoint_round_trip_on_device(tn, tmp_path):
-    """write_mps / read_mps (the GMPS group layout of gmps.jl:359-383 in an
-    .npz archive) on a device MPS after a DMRG run: the read-back state has
-    the same tensors, centre and energy."""
+@pytest.mark.parametrize("ext", [".npz", ".h5"])
+def test_mps_checkpoint_round_trip_on_device(tn, tmp_path, ext):
+    """write_mps / read_mps (the GMPS group layout of gmps.jl:359-383, as an
+    HDF5 file or an .npz archive) on a device MPS after a DMRG run: the
+    read-back state has the same tensors, centre and energy."""
     N = 8
     st = tn.spinhalf()
     W = tn.MPO(st, _tfim(tn, N))
     po = O.random_mps(2, N, 4, np.random.default_rng(3))
     psi = tn.GMPS.from_tensors(po.tensors, po.center)
     _, E = tn.dmrg(psi, W, maxdim=16, cutoff=1e-12, minsweeps=2, maxsweeps=2, verbose=False)
-    path = str(tmp_path / "state.npz")
+    path = str(tmp_path / ("state" + ext))
     tn.write_mps(path, psi, name="ground")
     back = tn.read_mps(path, name="ground")
     assert back.center == psi.center and back.bonddims() == psi.bonddims()
