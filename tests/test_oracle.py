@@ -458,3 +458,127 @@ def test_mpo_algebra_and_thermal_state_match_dense():
     ev = np.linalg.eigvalsh(Hd)
     w = np.exp(-beta * ev)
     assert abs(E - np.sum(w * ev) / np.sum(w)) < 1e-4
+
+
+def _complex_mps(rng, N, D, d=2):
+    dims = [1] + [min(D, d ** min(i, N - i)) for i in range(1, N)] + [1]
+    ts = [O.fr(rng.standard_normal((dims[i], d, dims[i + 1]))
+               + 1j * rng.standard_normal((dims[i], d, dims[i + 1])), (dims[i], d, dims[i + 1]))
+          for i in range(N)]
+    return O.GMPS(1, d, ts, 0)
+
+
+def _schmidt(vec, N, bond, d=2):
+    """Schmidt coefficients of a normalised dense state across (bond, bond+1);
+    the dense vector is column-major, site 1 fastest."""
+    M = O.fr(vec / np.linalg.norm(vec), (d ** bond, d ** (N - bond)))
+    return np.linalg.svd(M, compute_uv=False)
+
+
+def test_gauge_moves_match_dense_state():
+    """movecenter! (gmps.jl:60-112) without truncation keeps the dense state
+    and leaves the sites left of the centre left-orthonormal and those right
+    of it right-orthonormal."""
+    rng = np.random.default_rng(11)
+    N = 7
+    psi = _complex_mps(rng, N, 5)
+    v0 = X.mps_to_dense(psi)
+    for c in (4, 1, N, 3):
+        psi.movecenter(c)
+        assert psi.center == c
+        assert np.allclose(X.mps_to_dense(psi), v0, atol=1e-12 * np.linalg.norm(v0))
+        for i in range(1, N + 1):
+            A = psi[i]
+            if i < c:
+                M = O.fr(A, (-1, A.shape[2]))
+                assert np.allclose(M.conj().T @ M, np.eye(A.shape[2]), atol=1e-12)
+            elif i > c:
+                M = O.fr(A, (A.shape[0], -1))
+                assert np.allclose(M @ M.conj().T, np.eye(A.shape[0]), atol=1e-12)
+
+
+def test_entropy_and_spectra_match_dense_schmidt_values():
+    """entropy(psi, i) (gmps.jl:184-189) is -sum s^2 ln s^2 of the dense
+    state's Schmidt values across bond i; a product state gives 0 and a
+    GHZ state ln 2 at every bond."""
+    rng = np.random.default_rng(12)
+    N = 8
+    psi = _complex_mps(rng, N, 6)
+    psi.normalize()
+    v = X.mps_to_dense(psi)
+    for bond in range(1, N):
+        s = _schmidt(v, N, bond)
+        s = s[s > 1e-14]
+        assert abs(psi.entropy(bond) - float(-np.sum(s ** 2 * np.log(s ** 2)))) < 1e-10
+        sv = psi.singular_values(bond)
+        assert np.allclose(np.sort(sv)[::-1][:len(s)], s, atol=1e-12)
+    prod = O.product_mps(O.spinhalf(), ["up", "dn"] * 3)
+    assert all(abs(prod.entropy(b)) < 1e-14 for b in range(1, 6))
+    ghz = []
+    for i in range(N):
+        t = np.zeros((1 if i == 0 else 2, 2, 1 if i == N - 1 else 2), dtype=np.complex128)
+        for k in range(2):
+            t[0 if i == 0 else k, k, 0 if i == N - 1 else k] = 1.0
+        ghz.append(t)
+    g = O.GMPS(1, 2, ghz, 0)
+    g.normalize()
+    assert all(abs(g.entropy(b) - np.log(2)) < 1e-12 for b in range(1, N))
+
+
+@pytest.mark.parametrize("direction", [False, True])
+def test_replacesites_matches_dense_split(direction):
+    """replacesites! (gmps.jl:199-267): an untruncated split keeps the dense
+    state with theta in place; truncated to k it keeps theta's k largest
+    singular values, and the centre lands where the reference puts it."""
+    rng = np.random.default_rng(13)
+    N, site = 5, 2
+    psi = _complex_mps(rng, N, 4)
+    psi.movecenter(site)
+    Dl, Dr = psi[site].shape[0], psi[site + 1].shape[2]
+    theta = rng.standard_normal((Dl, 2, 2, Dr)) + 1j * rng.standard_normal((Dl, 2, 2, Dr))
+    ref = O.GMPS(1, 2, [psi[i] for i in range(1, N + 1)], psi.center)
+    # the dense state with theta in place of sites (site, site+1)
+    left = ref[1]
+    for i in range(2, site):
+        left = np.tensordot(left, ref[i], axes=([left.ndim - 1], [0]))
+    full = np.tensordot(left, theta, axes=([left.ndim - 1], [0]))
+    for i in range(site + 2, N + 1):
+        full = np.tensordot(full, ref[i], axes=([full.ndim - 1], [0]))
+    dense = O.fr(full[0, ..., 0], (-1,))
+    a = O.GMPS(1, 2, [ref[i] for i in range(1, N + 1)], ref.center)
+    a.replacesites(theta, site, direction)
+    assert a.center == (site if direction else site + 1)
+    assert np.allclose(X.mps_to_dense(a), dense, atol=1e-12 * np.linalg.norm(dense))
+    s = np.linalg.svd(O.fr(theta, (Dl * 2, 2 * Dr)), compute_uv=False)
+    k = 2
+    b = O.GMPS(1, 2, [ref[i] for i in range(1, N + 1)], ref.center)
+    b.replacesites(theta, site, direction, maxdim=k)
+    c = b[b.center]
+    # the centre holds U S: [Dl, s1, k] at the left site (direction true),
+    # [k, s2, Dr] at the right one
+    kept = np.linalg.svd(O.fr(c, (-1, c.shape[2])) if direction else O.fr(c, (c.shape[0], -1)),
+                         compute_uv=False)
+    assert np.allclose(np.sort(kept)[::-1][:k], s[:k], rtol=1e-12)
+    assert b[site].shape[2] == k
+
+
+def test_emission_rates_match_dense_expectations():
+    """qjmc_emission_rates (qjmc.jl:170-220): |c^2 <psi|L^dag L|psi>| for a
+    normalised state equals the dense expectation of each channel."""
+    rng = np.random.default_rng(14)
+    N = 6
+    psi = _complex_mps(rng, N, 4)
+    psi.normalize()
+    v = X.mps_to_dense(psi)
+    st = O.spinhalf()
+    Lj = O.OpList(N)
+    for i in range(1, N + 1):
+        Lj.add("s-", i, np.sqrt(0.1 * i))
+    Lj.add("z", 3, 0.5)
+    rates = O.qjmc_emission_rates(st, psi, Lj)
+    for k in range(len(Lj.ops)):
+        single = O.OpList(N)
+        single.add(Lj.ops[k][0], Lj.sites[k][0], 1.0)
+        Ld = X.oplist_to_dense(st, single)
+        ex = abs(Lj.coeffs[k]) ** 2 * np.real(np.vdot(Ld @ v, Ld @ v))
+        assert abs(rates[k] - ex) < 1e-12
