@@ -582,3 +582,54 @@ def test_emission_rates_match_dense_expectations():
         Ld = X.oplist_to_dense(st, single)
         ex = abs(Lj.coeffs[k]) ** 2 * np.real(np.vdot(Ld @ v, Ld @ v))
         assert abs(rates[k] - ex) < 1e-12
+
+
+def test_trotter_rows_converge_at_second_order():
+    """trotterize(...; order=2) (gatelist.jl:75-121): [odd(dt/2), even(dt),
+    odd(dt/2)] rows applied to a dense state approach exp(-iHT) with an
+    error falling as dt^2 (order=1: as dt)."""
+    import scipy.linalg as sla
+    st = O.spinhalf()
+    N, T = 6, 0.4
+    H = xxz(N, 1.0, 0.5, lambda i: 0.3 * i)
+    v0 = X.mps_to_dense(O.product_mps(st, ["up" if i % 2 else "dn" for i in range(1, N + 1)]))
+    exact = sla.expm(-1j * T * X.oplist_to_dense(st, H)) @ v0
+    for order, rate in ((2, 4.0), (1, 2.0)):
+        errs = []
+        for n in (8, 16):
+            rows = O.trotterize(st, H, T / n, order=order, evol="real")
+            v = v0
+            for _ in range(n):
+                v = X.apply_rows_dense(v, rows, N, 2)
+            errs.append(np.linalg.norm(v - exact))
+        assert abs(errs[0] / errs[1] - rate) < 0.1 * rate, (order, errs)  # 4.007 and 2.012
+
+
+def test_qjmc_gates_give_the_no_jump_evolution():
+    """qjmc_gates (qjmc.jl:9-26): the Trotter rows of H_eff = -iH - 1/2 sum
+    c^2 L^dag L (imaginary-time gates exp(dt H_eff)) applied to a dense
+    state match exp(T H_eff), the unnormalised no-jump evolution, to the
+    second-order Trotter error."""
+    import scipy.linalg as sla
+    st = O.spinhalf()
+    N, T, n = 4, 0.3, 30
+    H = O.OpList(N)
+    for i in range(1, N):
+        H.add(["z", "z"], [i, i + 1], 1.0)
+    for i in range(1, N + 1):
+        H.add("x", i, 0.8)
+    Lj = O.OpList(N)
+    for i in range(1, N + 1):
+        Lj.add("s-", i, np.sqrt(0.5))
+    heff, rows = O.qjmc_gates(st, H, Lj, T / n)
+    Hd = X.oplist_to_dense(st, H)
+    Ld = [np.sqrt(0.5) * X.oplist_to_dense(st, _single(N, "s-", i)) for i in range(1, N + 1)]
+    Heff = -1j * Hd - 0.5 * sum(L.conj().T @ L for L in Ld)
+    assert np.allclose(X.oplist_to_dense(st, heff), Heff, atol=1e-14)
+    v0 = X.mps_to_dense(O.product_mps(st, ["up"] * N))
+    v = v0
+    for _ in range(n):
+        v = X.apply_rows_dense(v, rows, N, 2)
+    exact = sla.expm(T * Heff) @ v0
+    assert np.linalg.norm(v - exact) < 1e-3 * np.linalg.norm(exact)
+    assert abs(np.linalg.norm(v) ** 2 - np.linalg.norm(exact) ** 2) < 1e-3
