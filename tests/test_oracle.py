@@ -633,3 +633,44 @@ def test_qjmc_gates_give_the_no_jump_evolution():
     exact = sla.expm(T * Heff) @ v0
     assert np.linalg.norm(v - exact) < 1e-3 * np.linalg.norm(exact)
     assert abs(np.linalg.norm(v) ** 2 - np.linalg.norm(exact) ** 2) < 1e-3
+
+
+def _fixture_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_oracle_fixtures", os.path.join(GOLDEN, "make_oracle_fixtures.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_oracle_reproduces_its_committed_outputs():
+    """tests/golden/oracle_outputs.json holds the parity cases' explicit
+    inputs (randomGMPS draws, uniform streams) and the oracle's outputs;
+    recomputing from the stored inputs gives the stored outputs (energies
+    1e-10 relative, spectra, entropies and <Z_i> 1e-9, bond dimensions and
+    jump records identical)."""
+    m = _fixture_module()
+    with open(os.path.join(GOLDEN, "oracle_outputs.json")) as f:
+        fx = json.load(f)
+    for name in ("dmrg_tfim_N20_config1", "dmrg_xxz_N16"):
+        c = fx[name]
+        E, dims, S, ent, z = m.run_dmrg_case(c)
+        assert abs(E - c["energy_last_lanczos"]) <= 1e-10 * abs(E), name
+        assert dims == c["bonddims"], name
+        assert np.allclose(S, c["singular_values"], atol=1e-9), name
+        assert abs(ent - c["entropy_bond"]) < 1e-9 and np.allclose(z, c["z"], atol=1e-9), name
+    c = fx["tebd_xxz_N16_quench"]
+    z, ln, dims, ent = m.run_tebd_case(c)
+    assert np.allclose(z, c["z_per_step"], atol=1e-9) and np.allclose(ln, c["lognorm"], atol=1e-9)
+    assert dims == c["bonddims"] and abs(ent - c["entropy_mid"]) < 1e-9
+    for name in ("qjmc_ising_N8_classical", "qjmc_ising_N8_norm_based"):
+        c = fx[name]
+        j, t, z = m.run_qjmc_case(c)
+        assert j == c["jumps"] and len(j) > 0, name
+        assert np.allclose(t, c["jump_times"], rtol=0, atol=1e-12), name
+        assert np.allclose(z, c["z_per_step"], atol=1e-9), name
+    # the stored randomGMPS draws are the seeded ones the parity tests use
+    dr = m.seeded_draws(20, 4, 1)
+    assert all(np.array_equal(a, m.dec(e)) for a, e in
+               zip(dr, fx["dmrg_tfim_N20_config1"]["randomMPS_draws"]))
