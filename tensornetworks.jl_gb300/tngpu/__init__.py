@@ -18,8 +18,10 @@ from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEB
                          philox_uniforms, qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation,
                          shard_range, tebd, tune_qjmc_width,
                          tebd_grad, trotterize, vmps)
-from .models import OpList, Sitetypes, gate_exp, mpo_tensors, spinhalf, trotter_rows  # noqa: F401
-from .mps import (GMPO, GMPS, MPO, MPOHandle, MPSProjector, adjoint, applyMPO, as_gmpo,  # noqa: F401
-                  entropy, inner, mpo_product, productMPO, trace,
-                  mps_from_record, mps_record, overlap, productMPS, randomMPS, read_mps,
-                  write_mps)
+from .models import (OpList, Sitetypes, dag, gate_exp, mpo_tensors, op, siteindexs,  # noqa: F401
+                     siterange, sitetensor, spinhalf, state, totensor, trotter_rows)
+from .mps import (GMPO, GMPS, MPO, MPOHandle, MPSProjector, adjoint, applyMPO, applyop,  # noqa: F401
+                  as_gmpo, bonddim, center, dim, entropy, inner, ismpo, ismps, maxbonddim,
+                  movecenter, mpo_product, norm, normalize, productMPO, rank, tensors, trace,
+                  truncate, mps_from_record, mps_record, overlap, productMPS, randomMPS,
+                  read_mps, write_mps)

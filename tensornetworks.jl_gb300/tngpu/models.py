@@ -170,6 +170,39 @@ def site_tensor(st, H, site):
     return sum(term_tensor(st, H, k) for k in ks)
 
 
+# Free-function forms of the reference's OpList and Sitetypes functions
+# (oplist.jl:102-183, sitetypes.jl:144-166); term and site indices 1-based
+# as there.
+def siterange(H):
+    return H.siterange()
+
+
+def siteindexs(H, site):
+    """1-based indices of the terms starting at ``site`` (oplist.jl:117-125)."""
+    return [k + 1 for k in H.siteindexs(site)]
+
+
+def totensor(H, st, idx):
+    """Term ``idx`` (1-based) as a tensor (oplist.jl:134-156)."""
+    return term_tensor(st, H, idx - 1)
+
+
+def sitetensor(H, st, site):
+    return site_tensor(st, H, site)
+
+
+def op(st, name):
+    return st.op(name)
+
+
+def dag(st, name):
+    return st.dag(name)
+
+
+def state(st, name):
+    return st.state(name)
+
+
 # ---------------------------------------------------------------------------
 # MPO from an operator list
 # ---------------------------------------------------------------------------

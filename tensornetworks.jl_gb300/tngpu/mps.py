@@ -396,6 +396,9 @@ def inner(st, psi, oplist, phi):
     return out
 
 
+# Free-function forms of the reference's accessors and gauge operations
+# (abstractmps.jl:4-81, gmps.jl:29-127, mps.jl:141-151), for code written
+# against the reference's function names; each calls the object's method.
 def entropy(psi, site):
     return psi.entropy(site)
 
@@ -406,6 +409,63 @@ def normalize(psi):
 
 def movecenter(psi, idx, **kw):
     psi.movecenter(idx, **kw)
+
+
+def norm(psi):
+    return psi.norm()
+
+
+def dim(psi):
+    return psi.dim
+
+
+def rank(psi):
+    return psi.rank
+
+
+def center(psi):
+    return psi.center
+
+
+def tensors(psi):
+    return psi.tensors()
+
+
+def bonddim(psi, site):
+    """The bond dimension between site and site+1 (abstractmps.jl:64-67):
+    None for a site outside 1..N; site N has no bond to its right."""
+    if site < 1 or site > len(psi):
+        return None
+    if site == len(psi):
+        raise IndexError("no bond to the right of the last site")
+    return psi.bonddims()[site]
+
+
+def maxbonddim(psi):
+    return psi.maxbonddim()
+
+
+def ismps(psi):
+    return psi.rank == 1
+
+
+def ismpo(psi):
+    return psi.rank == 2
+
+
+def truncate(psi, **kw):
+    """truncate! (gmps.jl:121-127): a truncating sweep from the centre at
+    one end to the other end.  With the centre elsewhere the reference's
+    movecenter!(psi, 0) raises, and so does this."""
+    N = len(psi)
+    if psi.center != 1 and psi.center != N:
+        raise ValueError("The index is out of range.")
+    psi.movecenter(N if psi.center == 1 else 1, **kw)
+
+
+def applyop(st, psi, ops, sites):
+    """applyop!(st, psi, ops, sites) (mps.jl:141-151)."""
+    psi.applyop(st, ops, sites)
 
 
 # ---------------------------------------------------------------------------

@@ -350,3 +350,62 @@ def test_julia_shim_ccalls_match_header():
         assert name in decl, name
         kinds = [_jl_kind(t) for t in _split_top(_balanced(src, m.end() - 1))]
         assert kinds == decl[name], (name, kinds, decl[name])
+
+
+def test_reference_free_functions():
+    """The free-function forms of the reference's accessors and OpList /
+    Sitetypes functions dispatch to the objects' methods with the
+    reference's 1-based indices and errors (abstractmps.jl:64-81,
+    gmps.jl:121-127, oplist.jl:102-183)."""
+    import tngpu as tn
+    from tngpu import models as Mo
+
+    class State:
+        rank, dim = 1, 2
+
+        def __init__(self, center):
+            self.center, self.calls = center, []
+
+        def __len__(self):
+            return 4
+
+        def bonddims(self):
+            return [1, 2, 4, 2, 1]
+
+        def maxbonddim(self):
+            return 4
+
+        def tensors(self):
+            return ["t"]
+
+        def norm(self):
+            return 1.5
+
+        def movecenter(self, idx, **kw):
+            self.calls.append((idx, kw))
+            self.center = idx
+
+    s = State(1)
+    assert (tn.dim(s), tn.rank(s), tn.center(s), tn.tensors(s), tn.norm(s)) == (2, 1, 1, ["t"], 1.5)
+    assert [tn.bonddim(s, i) for i in (0, 1, 2, 3, 5)] == [None, 2, 4, 2, None]
+    with pytest.raises(IndexError):
+        tn.bonddim(s, 4)
+    assert tn.maxbonddim(s) == 4 and tn.ismps(s) and not tn.ismpo(s)
+    tn.truncate(s, maxdim=3)
+    assert s.calls == [(4, {"maxdim": 3})]
+    tn.truncate(s)
+    assert s.calls[-1] == (1, {})
+    s.center = 2
+    with pytest.raises(ValueError, match="out of range"):
+        tn.truncate(s)
+    st = tn.spinhalf()
+    H = tn.OpList(5)
+    H.add(["z", "z"], [2, 3], 0.5)
+    H.add("x", 2, 2.0)
+    H.add(["x", "z"], [1, 3], 1.0)
+    assert tn.siterange(H) == 3 and tn.siteindexs(H, 2) == [1, 2] and tn.siteindexs(H, 5) == []
+    assert np.array_equal(tn.totensor(H, st, 2), Mo.term_tensor(st, H, 1))
+    assert np.array_equal(tn.sitetensor(H, st, 2), Mo.site_tensor(st, H, 2))
+    assert tn.sitetensor(H, st, 4) is None
+    assert np.array_equal(tn.op(st, "s+"), st.op("s+")) and tn.dag(st, "s+") == st.dag("s+")
+    assert np.array_equal(tn.state(st, "up"), st.state("up"))
