@@ -3,8 +3,10 @@
 The names mirror the reference's exports (src/exports.jl): ``spinhalf``,
 ``OpList``, ``MPO``, ``randomMPS``, ``productMPS``, ``dmrg``,
 ``trotterize``, ``applygates``, ``tebd``, ``qjmc_simulation``, ``inner``,
-observers, and the MPO algebra (``productMPO``, ``applyMPO``, ``adjoint``,
-``trace``).  Every contraction, truncation and eigensolve runs in
+observers, the MPO algebra (``productMPO``, ``applyMPO``, ``adjoint``,
+``trace``), and free-function forms of the accessors and OpList/Sitetypes
+functions (``center``, ``bonddim``, ``movecenter``, ``truncate``,
+``applyop``, ``sitetensor``, ``op`` ...).  Every contraction, truncation and eigensolve runs in
 ``libtngpu.so`` on the GPU; nothing here computes on the CPU beyond building
 model inputs (operator tables, MPO tensors, 4x4 gate exponentials and their
 output-index lifts) and re-laying out MPO sites for ``adjoint``.
