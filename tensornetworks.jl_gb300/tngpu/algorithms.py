@@ -638,14 +638,22 @@ class QJMCOperators:
 
 
 class QJMCActivity:
-    """qjmc.jl:264-285 (HDF5 saving is outside this path)."""
+    """qjmc.jl:264-285: the time and jump count of the last measurement;
+    with ``save`` each measurement rewrites the HDF5 file ``savefile`` with
+    the datasets "time" (Float64) and "jumps" (Int64), as h5open(savefile,
+    "w") does there."""
 
     def __init__(self, save=False, savefile=""):
         self.time, self.jumps = 0.0, 0
+        self.save, self.savefile = bool(save), savefile
 
     def measure(self, time, psi, jumps, jumptimes):
         self.time = time
         self.jumps = len(jumps)
+        if self.save:
+            from . import h5
+            h5.write_file(self.savefile, h5.Group({"time": float(self.time),
+                                                   "jumps": int(self.jumps)}))
 
 
 class QJMCEntropy:

@@ -1,4 +1,5 @@
-"""HDF5 checkpoints of GMPS objects, in the layout of gmps.jl:359-383.
+"""HDF5 files in HDF5.jl's layout: GMPS checkpoints (gmps.jl:359-383) and
+the record of QJMCActivity (qjmc.jl:275-284).
 
 The reference saves a GMPS with HDF5.jl as one group holding:
 
@@ -132,69 +133,120 @@ class _Group:
         return out + b"\0" * (self.sizes["snod"] - len(out))
 
     def tree(self, snod_addr):
-        out = b"TREE" + struct.pack("<BBHQQ", 0, 0, 1, UNDEF, UNDEF)
-        out += struct.pack("<QQQ", 0, snod_addr, self.offset[self.names[-1]])
+        """A leaf B-tree node over the one symbol-table node, or with no
+        children for an empty group."""
+        used = 0 if snod_addr is None else 1
+        out = b"TREE" + struct.pack("<BBHQQ", 0, 0, used, UNDEF, UNDEF) + struct.pack("<Q", 0)
+        if used:
+            out += struct.pack("<QQ", snod_addr, self.offset[self.names[-1]])
         return out + b"\0" * (self.sizes["tree"] - len(out))
 
 
-def write_gmps(path, tensors, center, name="psi"):
-    """Write one GMPS group ``name`` (gmps.jl:359-370) as a new HDF5 file.
-    ``tensors``: the site arrays, [Dl, d, Dr] or [Dl, d, d, Dr] complex."""
-    tensors = [np.asarray(t, dtype=np.complex128) for t in tensors]
-    N = len(tensors)
-    if N == 0:
-        raise ValueError("an MPS needs at least one site")
-    dsets = [("length", _dt_int64(), (), struct.pack("<q", N)),
-             ("center", _dt_int64(), (), struct.pack("<q", int(center)))]
-    for i, t in enumerate(tensors, start=1):
-        dsets.append((f"MPS[{i}]", _dt_complex(), tuple(reversed(t.shape)),
-                      np.asfortranarray(t).tobytes(order="F")))
-    leaf_k = max(4, -(-len(dsets) // 2))
-    grp, root = _Group([d[0] for d in dsets], leaf_k), _Group([name], leaf_k)
+class Group:
+    """A group to write: ``members`` maps names to sub-Groups or dataset
+    values, ``attrs`` names to attribute values.  Values follow HDF5.jl's
+    conventions: str (fixed-length string), int (Int64), float (Float64),
+    and numpy arrays or scalars of integers, floats or complex numbers
+    (column-major arrays stored with their dimensions reversed)."""
 
+    def __init__(self, members=None, attrs=None):
+        self.members = dict(members or {})
+        self.attrs = dict(attrs or {})
+
+
+def _encode(v):
+    """(datatype, HDF5 dims, raw bytes) of a value."""
+    if isinstance(v, str):
+        b = v.encode() + b"\0"
+        return _dt_string(len(b)), (), b
+    if isinstance(v, (bool, np.bool_)):
+        raise TypeError("booleans have no HDF5.jl counterpart here")
+    if isinstance(v, (int, np.integer)):
+        return _dt_int64(), (), struct.pack("<q", int(v))
+    if isinstance(v, (float, np.floating)):
+        return _dt_f64(), (), struct.pack("<d", float(v))
+    a = np.asarray(v)
+    if np.iscomplexobj(a):
+        a, dt = a.astype(np.complex128), _dt_complex()
+    elif a.dtype.kind == "f":
+        a, dt = a.astype(np.float64), _dt_f64()
+    elif a.dtype.kind in "iu":
+        a, dt = a.astype(np.int64), _dt_int64()
+    else:
+        raise TypeError(f"cannot store values of dtype {a.dtype}")
+    if a.ndim == 0:
+        return dt, (), a.tobytes()
+    return dt, tuple(reversed(a.shape)), np.asfortranarray(a).tobytes(order="F")
+
+
+def write_file(path, root):
+    """Write the Group ``root`` and everything under it as a new HDF5 file."""
+    def most(g):
+        subs = [most(m) for m in g.members.values() if isinstance(m, Group)]
+        return max([len(g.members)] + subs)
+
+    leaf_k = max(4, -(-most(root) // 2))  # each group's entries fit one node
     eof = 96  # the superblock
+    writes = []
+
     def reserve(size):
         nonlocal eof
         addr = eof
         eof += -(-size // 8) * 8
         return addr
 
-    placed = []
-    for dname, dt, dims, raw in dsets:
-        hdr = reserve(len(_dataset_header(dt, dims, 0, len(raw))))
-        placed.append((dname, dt, dims, raw, hdr, reserve(len(raw))))
-    g_heap, g_snod, g_tree = (reserve(grp.sizes[k]) for k in ("heap", "snod", "tree"))
-    sdt = _dt_string(4)
-    attrs = [_attr_msg("type", sdt, _space(()), b"MPS\0"),
-             _attr_msg("version", _dt_int64(), _space(()), struct.pack("<q", 1))]
-    g_hdr_bytes = _object_header([_msg(_STAB, struct.pack("<QQ", g_tree, g_heap))] + attrs)
-    g_hdr = reserve(len(g_hdr_bytes))
-    r_heap, r_snod, r_tree = (reserve(root.sizes[k]) for k in ("heap", "snod", "tree"))
-    r_hdr_bytes = _object_header([_msg(_STAB, struct.pack("<QQ", r_tree, r_heap))])
-    r_hdr = reserve(len(r_hdr_bytes))
+    def place(g):
+        """Lay out g's members, then g; (object header, B-tree, heap)."""
+        st = _Group(list(g.members), leaf_k)
+        entries = {}
+        for name, m in g.members.items():
+            if isinstance(m, Group):
+                entries[name] = _entry(st.offset[name], *place(m))
+                continue
+            dt, dims, raw = _encode(m)
+            hdr = reserve(len(_dataset_header(dt, dims, 0, len(raw))))
+            data = reserve(len(raw))
+            writes.append((hdr, _dataset_header(dt, dims, data, len(raw))))
+            writes.append((data, raw))
+            entries[name] = _entry(st.offset[name], hdr)
+        heap = reserve(st.sizes["heap"])
+        tree = reserve(st.sizes["tree"])
+        writes.append((heap, st.heap(heap)))
+        if entries:
+            snod = reserve(st.sizes["snod"])
+            writes.append((snod, st.snod(entries)))
+            writes.append((tree, st.tree(snod)))
+        else:
+            writes.append((tree, st.tree(None)))
+        attrs = []
+        for k, v in g.attrs.items():
+            dt, dims, raw = _encode(v)
+            attrs.append(_attr_msg(k, dt, _space(dims), raw))
+        hdr_bytes = _object_header([_msg(_STAB, struct.pack("<QQ", tree, heap))] + attrs)
+        hdr = reserve(len(hdr_bytes))
+        writes.append((hdr, hdr_bytes))
+        return hdr, tree, heap
 
+    r_hdr, r_tree, r_heap = place(root)
     buf = bytearray(eof)
-    def put(addr, b):
+    for addr, b in writes:
         buf[addr:addr + len(b)] = b
-
-    entries = {}
-    for dname, dt, dims, raw, hdr, data in placed:
-        put(hdr, _dataset_header(dt, dims, data, len(raw)))
-        put(data, raw)
-        entries[dname] = _entry(grp.offset[dname], hdr)
-    put(g_heap, grp.heap(g_heap))
-    put(g_snod, grp.snod(entries))
-    put(g_tree, grp.tree(g_snod))
-    put(g_hdr, g_hdr_bytes)
-    put(r_heap, root.heap(r_heap))
-    put(r_snod, root.snod({name: _entry(root.offset[name], g_hdr, g_tree, g_heap)}))
-    put(r_tree, root.tree(r_snod))
-    put(r_hdr, r_hdr_bytes)
     sb = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", leaf_k, BTREE_K, 0)
     sb += struct.pack("<QQQQ", 0, UNDEF, eof, UNDEF) + _entry(0, r_hdr, r_tree, r_heap)
-    put(0, sb)
+    buf[:len(sb)] = sb
     with open(path, "wb") as f:
         f.write(bytes(buf))
+
+
+def write_gmps(path, tensors, center, name="psi"):
+    """Write one GMPS group ``name`` (gmps.jl:359-370) as a new HDF5 file.
+    ``tensors``: the site arrays, [Dl, d, Dr] or [Dl, d, d, Dr] complex."""
+    if len(tensors) == 0:
+        raise ValueError("an MPS needs at least one site")
+    members = {"length": len(tensors), "center": int(center)}
+    for i, t in enumerate(tensors, start=1):
+        members[f"MPS[{i}]"] = np.asarray(t, dtype=np.complex128)
+    write_file(path, Group({name: Group(members, {"type": "MPS", "version": 1})}))
 
 
 # ---- reading -------------------------------------------------------------------------
@@ -369,3 +421,20 @@ def read_gmps(path, name="psi"):
     N = int(r.dataset(members["length"]))
     center = int(r.dataset(members["center"]))
     return [r.dataset(members[f"MPS[{i}]"]) for i in range(1, N + 1)], center
+
+
+def read_file(path):
+    """Every dataset of an HDF5 file, as nested dicts by group."""
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+
+    def walk(addr):
+        out = {}
+        for name, a in r.group(addr).items():
+            if any(t == _STAB for t, _ in r.messages(a)):
+                out[name] = walk(a)
+            else:
+                out[name] = r.dataset(a)
+        return out
+
+    return walk(r.root)

@@ -211,3 +211,43 @@ def test_write_mps_read_mps_dispatch(tmp_path, monkeypatch, ext):
         assert c is cls and center == 1 and all(np.array_equal(a, b) for a, b in zip(ts, back))
     with open(path, "rb") as f:
         assert (f.read(8) == h5.SIGNATURE) == (ext != ".npz")
+
+
+def test_group_trees_round_trip(tmp_path):
+    """write_file/read_file: nested groups (one empty), Int64/Float64
+    scalars, real, integer and complex arrays in column-major order,
+    group attributes."""
+    rng = np.random.default_rng(7)
+    real = np.asfortranarray(rng.standard_normal((3, 5)))
+    ints = np.arange(12).reshape(3, 4)
+    cplx = crand(rng, 2, 3, 4)
+    p = str(tmp_path / "tree.h5")
+    h5.write_file(p, h5.Group({
+        "a": 3, "b": 2.5, "real": real, "ints": ints,
+        "sub": h5.Group({"c": cplx, "deeper": h5.Group({"z": 1j}), "empty": h5.Group()},
+                        attrs={"note": "x", "n": 7, "w": 0.25})}))
+    got = h5.read_file(p)
+    assert got["a"] == 3 and got["b"] == 2.5
+    assert np.array_equal(got["real"], real) and np.array_equal(got["ints"], ints)
+    assert np.array_equal(got["sub"]["c"], cplx) and got["sub"]["deeper"]["z"] == 1j
+    assert got["sub"]["empty"] == {}
+    r = h5._Reader(open(p, "rb").read())
+    assert r.attributes(r.group(r.root)["sub"]) == {"note": "x", "n": 7, "w": 0.25}
+    with pytest.raises(TypeError):
+        h5.write_file(p, h5.Group({"flag": True}))
+
+
+def test_qjmc_activity_saves_time_and_jumps(tmp_path):
+    """QJMCActivity(save=true, savefile) (qjmc.jl:275-284) rewrites the file
+    with "time" and "jumps" at every measurement."""
+    import tngpu as tn
+    p = str(tmp_path / "activity.h5")
+    obs = tn.QJMCActivity(True, p)
+    obs.measure(0.5, None, [3], [0.2])
+    assert h5.read_file(p) == {"time": 0.5, "jumps": 1}
+    obs.measure(1.25, None, [3, 1, 2], [0.2, 0.9, 1.1])
+    got = h5.read_file(p)
+    assert got == {"time": 1.25, "jumps": 3} and isinstance(got["jumps"], np.integer)
+    quiet = tn.QJMCActivity()
+    quiet.measure(1.0, None, [], [])
+    assert (quiet.time, quiet.jumps) == (1.0, 0)
