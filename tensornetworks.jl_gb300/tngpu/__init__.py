@@ -20,7 +20,7 @@ from .algorithms import (GateList, QJMCActivity, QJMCEntropy, QJMCOperators, TEB
                          philox_uniforms, qjmc_ensemble, qjmc_ensemble_sharded, qjmc_simulation,
                          shard_range, tebd, tune_qjmc_width,
                          tebd_grad, trotterize, vmps)
-from .models import (OpList, Sitetypes, dag, gate_exp, mpo_tensors, op, siteindexs,  # noqa: F401
+from .models import (OpList, Sitetypes, dag, gate_exp, gatesize, mpo_tensors, op, siteindexs,  # noqa: F401
                      siterange, sitetensor, spinhalf, state, totensor, trotter_rows)
 from .mps import (GMPO, GMPS, MPO, MPOHandle, MPSProjector, adjoint, applyMPO, applyop,  # noqa: F401
                   as_gmpo, bonddim, center, dim, entropy, inner, ismpo, ismps, maxbonddim,

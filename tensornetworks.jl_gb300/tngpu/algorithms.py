@@ -14,7 +14,7 @@ import math
 import numpy as np
 
 from . import _lib as L
-from .models import OpList, trotter_rows, trotter_rows_dparam
+from .models import OpList, gatesize, trotter_rows, trotter_rows_dparam
 from .mps import GMPS, MPOHandle, MPSProjector, applyMPO, inner
 
 
@@ -137,7 +137,7 @@ class GateList:
         self.ctx = ctx or L.context()
         row_len = np.asarray([len(s) for s, _ in rows], dtype=np.int32)
         sites = np.asarray([s for ss, _ in rows for s in ss], dtype=np.int32)
-        nsites = np.asarray([g.ndim // 2 for _, gs in rows for g in gs], dtype=np.int32)
+        nsites = np.asarray([gatesize(g) for _, gs in rows for g in gs], dtype=np.int32)
         mats = [L.cplx_f(g) for _, gs in rows for g in gs]
         h = C.c_void_p()
         self.ctx.check(self.ctx.lib.tn_gates_upload(

@@ -191,6 +191,14 @@ def sitetensor(H, st, site):
     return site_tensor(st, H, site)
 
 
+def gatesize(gate):
+    """The number of sites a gate acts on (gatelist.jl:28-32)."""
+    n = np.ndim(gate)
+    if n % 2 == 1:
+        raise ValueError("The gate must have even number of dimensions.")
+    return n // 2
+
+
 def op(st, name):
     return st.op(name)
 

@@ -409,3 +409,6 @@ def test_reference_free_functions():
     assert tn.sitetensor(H, st, 4) is None
     assert np.array_equal(tn.op(st, "s+"), st.op("s+")) and tn.dag(st, "s+") == st.dag("s+")
     assert np.array_equal(tn.state(st, "up"), st.state("up"))
+    assert tn.gatesize(np.zeros((2, 2, 2, 2))) == 2 and tn.gatesize(np.zeros((2, 2))) == 1
+    with pytest.raises(ValueError, match="even number of dimensions"):
+        tn.gatesize(np.zeros((2, 2, 2)))
