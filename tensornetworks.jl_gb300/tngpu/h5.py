@@ -291,7 +291,8 @@ class _Reader:
         return out
 
     def heap_name(self, heap, off):
-        assert self.b[self.at(heap):self.at(heap) + 4] == b"HEAP"
+        if self.b[self.at(heap):self.at(heap) + 4] != b"HEAP":
+            raise ValueError("corrupt local heap")
         data = self.at(self.u64(self.at(heap) + 24))
         end = self.b.index(b"\0", data + off)
         return self.b[data + off:end].decode()
