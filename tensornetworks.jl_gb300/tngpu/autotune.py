@@ -14,6 +14,7 @@ the engine's CUDA-event launch time, and kept in a JSON cache.
 import json
 import os
 import tempfile
+import warnings
 
 WIDTHS = (1, 2, 4, 8)
 
@@ -88,5 +89,8 @@ def tune(key, probe, widths=WIDTHS, cache=None):
         timings[w] = t
     best = min(widths, key=lambda w: (timings[w], w))
     if cache is not None:
-        cache.put(key, best, timings)
+        try:
+            cache.put(key, best, timings)
+        except OSError as e:  # an unwritable cache costs a re-tune, not the run
+            warnings.warn(f"autotune cache {cache.path} not written: {e}")
     return best, timings

@@ -70,3 +70,12 @@ def test_default_cache_path_honours_environment(monkeypatch, tmp_path):
     monkeypatch.delenv("TNGPU_TUNE_CACHE")
     monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
     assert AT.default_cache_path() == str(tmp_path / "tngpu" / "engine_widths.json")
+
+
+def test_unwritable_cache_keeps_the_tuned_width(tmp_path):
+    blocker = tmp_path / "file"
+    blocker.write_text("")
+    cache = AT.WidthCache(str(blocker / "sub" / "w.json"))  # a directory under a file
+    with pytest.warns(UserWarning, match="not written"):
+        w, t = AT.tune("k", lambda w: {1: 2.0, 2: 1.0, 4: 3.0, 8: 4.0}[w], cache=cache)
+    assert w == 2 and len(t) == 4
