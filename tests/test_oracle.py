@@ -67,6 +67,12 @@ def test_svd_keep_rule():
     assert O.svd_keep(S, cutoff=0.9) == 1
     assert O.svd_keep(S, cutoff=0.9, mindim=3) == 3
     assert O.svd_keep(np.zeros(3), cutoff=1e-10) == 1
+    # a tail weight exactly at the cutoff is discarded: the comparison is
+    # strict (tensors.jl:211); equal singular values make the weights exact
+    S = np.ones(4)  # tail weights 1, 3/4, 1/2, 1/4
+    assert O.svd_keep(S, cutoff=0.5) == 2
+    assert O.svd_keep(S, cutoff=0.5 - 2.0 ** -40) == 3
+    assert O.svd_keep(S, cutoff=0.25) == 3 and O.svd_keep(S, cutoff=0.2) == 4
 
 
 def test_lanczos_converges_to_lowest():
