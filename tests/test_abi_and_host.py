@@ -412,3 +412,30 @@ def test_reference_free_functions():
     assert tn.gatesize(np.zeros((2, 2, 2, 2))) == 2 and tn.gatesize(np.zeros((2, 2))) == 1
     with pytest.raises(ValueError, match="even number of dimensions"):
         tn.gatesize(np.zeros((2, 2, 2)))
+
+
+def test_product_path_fails_loudly_without_a_gpu(built):
+    """No CPU fallback: where no GPU can be used, creating a context returns
+    TN_ERR_CUDA with the CUDA runtime's message, and every entry into the
+    product path (state upload, MPO upload, the algorithms) raises it."""
+    import tngpu as tn
+    from tngpu import _lib as L
+    TN_ERR_CUDA = -2  # include/tngpu.h
+    assert L.TN_ERR[TN_ERR_CUDA] == "CUDA error"
+    lib = L.load()
+    h = ctypes.c_void_p()
+    rc = lib.tn_ctx_create(0, ctypes.byref(h))
+    if rc == L.TN_OK:
+        lib.tn_ctx_destroy(h)
+        pytest.skip("a GPU is present")
+    assert rc == TN_ERR_CUDA and lib.tn_last_error(None).decode()
+    st = tn.spinhalf()
+    H = tn.OpList(4)
+    H.add(["z", "z"], [1, 2], 1.0)
+    for call in (lambda: tn.productMPS(st, ["up"] * 4),
+                 lambda: tn.MPO(st, H),
+                 lambda: tn.randomMPS(2, 4, 2, rng=np.random.default_rng(0)),
+                 lambda: tn.trotterize(st, H, 0.1)):
+        with pytest.raises(tn.TNError) as e:
+            call()
+        assert e.value.code == TN_ERR_CUDA
