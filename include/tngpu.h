@@ -3,7 +3,7 @@
  * finite-MPS hot path of TensorNetworks.jl (two-site DMRG, TEBD gate
  * application, quantum-jump Monte Carlo).
  *
- * Conventions (the reference's, structures/mps/*.jl):
+ * Conventions (the reference's, in its structures/mps sources):
  *   - every tensor is complex double, passed as interleaved (re, im) pairs in
  *     column-major (Julia) order;
  *   - MPS site  A[Dl, d, Dr]            (structures/mps/gmps.jl:8-13)

@@ -72,6 +72,7 @@ static thread_local std::string g_noctx_err;
     }                                                               \
     catch (const std::bad_alloc&) {                                 \
         if (_c) _c->err = "host allocation failed";                 \
+        else g_noctx_err = "host allocation failed";                \
         return TN_ERR_OOM;                                          \
     }                                                               \
     catch (const std::exception& e) {                               \
@@ -102,7 +103,6 @@ extern "C" {
 int32_t tn_version(void) { return 100; }
 
 int32_t tn_ctx_create(int32_t device, tn_ctx** out) {
-    tn::Ctx* _c = nullptr;
     try {
         TN_REQUIRE(out != nullptr, "null output pointer");
         int ndev = 0;
@@ -120,6 +120,12 @@ int32_t tn_ctx_create(int32_t device, tn_ctx** out) {
     } catch (const tn::Error& e) {
         g_noctx_err = e.what();
         return e.code;
+    } catch (const std::bad_alloc&) {
+        g_noctx_err = "host allocation failed";
+        return TN_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_noctx_err = e.what();
+        return TN_ERR_INVALID;
     }
 }
 
